@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 MC secant routing path.
+
+Metric: segment-steps per second (segments x routed time steps / s) of FP64
+Muskingum-Cunge secant tree routing at secant tolerance rtol = 1e-8
+(atol = 1e-10), default workload c1: a 2.7M-segment, ~1.1M-reach random binary
+river tree (~2,400 levels), 144 steps of dt = 300 s, seeded synthetic
+parameters and lateral inflow (no dataset is available offline).
+
+One bench "step" = one whole 144-step routing run of the network (the state
+carries over from run to run), replayed from a captured CUDA graph with the
+lateral inflow (3.1 GB, larger than L2) resident in HBM. `e2e` is the same
+metric through the public C ABI with host buffers: troute_run (copies the
+step's lateral inflow from pinned host memory) plus troute_get_state (copies
+the routed discharge, depth, velocity and reach outflow back).
+
+--impl reference times the reference's CPU algorithm (the oracle port of
+cpu_wavefront_fp64, all host threads, one routed time step of the same
+network per bench step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "noaa-gpu-kernels_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "segment-steps/s at 1e-8 depth tol: batched+warm-start vs plain MC, 1 GB300"
+UNIT = "seg-steps/s"
+TIGHT = dict(rtol=1e-8, atol=1e-10, maxiter=100, attempts=5)
+BYTES_PER_SEG_STEP = 112  # params 64 + qlat 8 + q 8 + depth 8 read; q, depth, velocity 24 written
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c1")
+    ap.add_argument("--n-ts", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------- distributed plumbing
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.gpu_id:
+            cmd += ["-i", self.gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- helpers
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic_per_seg_step():
+    """DRAM bytes per segment-step of route_kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "route_kernel_c1.md")
+    try:
+        for ln in open(p):
+            if ln.strip().startswith("dram_bytes_per_seg_step:"):
+                return float(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def workload(name: str, n_ts: int | None):
+    from troute_gb300 import synth
+
+    return synth.network(name, n_ts=n_ts)
+
+
+def cpu_baseline(w) -> dict:
+    """The oracle port of cpu_wavefront_fp64, one core, one routed step of the
+    same network from its initial state."""
+    from oracle import troute_oracle as O
+
+    O.build(ref=False)
+    tol = (TIGHT["rtol"], TIGHT["atol"], TIGHT["maxiter"], TIGHT["attempts"])
+    S = w["topo"]["n_segments"]
+    t0 = time.perf_counter()
+    O.route_tree(w["topo"], w["params"], w["qlat"][:1], w["q0"], w["d0"], w["rl0"], tol=tol, threads=1)
+    dt = time.perf_counter() - t0
+    return {"value": S / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"1 routed step of the {S}-segment network from its initial state, rtol 1e-8, "
+                      f"single thread ({dt:.1f} s)"}
+
+
+# --------------------------------------------------------------------------- reference arm
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    from oracle import troute_oracle as O
+
+    O.build(ref=False)
+    w = workload(args.workload, args.n_ts)
+    S = w["topo"]["n_segments"]
+    nth = os.cpu_count() or 1
+    tol = (TIGHT["rtol"], TIGHT["atol"], TIGHT["maxiter"], TIGHT["attempts"])
+    lp, lr = O.levels(w["topo"]["reach_up_ptr"], w["topo"]["reach_up_idx"], len(w["topo"]["reach_seg_start"]))
+    q, d, rl = w["q0"], w["d0"], w["rl0"]
+    T = w["qlat"].shape[0]
+    times = []
+    for k in range(args.warmup + args.steps):
+        t = k % T
+        t0 = time.perf_counter()
+        o = O.route_tree(w["topo"], w["params"], w["qlat"][t:t + 1], q, d, rl, tol=tol, threads=nth,
+                         level_ptr=lp, level_reach=lr)
+        el = time.perf_counter() - t0
+        q, d, rl = o["q"], o["d"], o["reach_last"]
+        if k >= args.warmup:
+            times.append(el)
+    tot = sum(times)
+    value = S * len(times) / tot
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": f"{args.workload}: FP64 MC secant tree routing, {S} segments, "
+                                   f"{len(w['topo']['reach_seg_start'])} reaches, rtol 1e-8; one routed step "
+                                   f"per bench step", "segments": S},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": f"1 routed time step of the {S}-segment network per bench step, "
+                                       f"{nth} threads (level-parallel oracle port of cpu_wavefront_fp64)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- our arm
+def run_ours(args, dist: Dist):
+    import torch
+
+    import troute_gb300 as T
+
+    dev = torch.device("cuda", dist.local if dist.world > 1 else 0)
+    torch.cuda.set_device(dev)
+    w = workload(args.workload, args.n_ts)
+    topo = w["topo"]
+    S, R = topo["n_segments"], len(topo["reach_seg_start"])
+    n_ts = w["qlat"].shape[0]
+    cfg = T.make_cfg(**TIGHT)
+    net = T.Network(topo, w["params"], cfg=cfg)
+    net.set_state(w["q0"], w["d0"], w["rl0"])
+    qlat_host = torch.empty((n_ts, S), dtype=torch.float64, pin_memory=True)
+    qlat_host.numpy()[:] = w["qlat"]
+    qlat_dev = qlat_host.to(dev, non_blocking=False)
+    stream = torch.cuda.current_stream(dev)
+    net.graph_capture(qlat_dev.data_ptr(), n_ts)
+    for _ in range(args.warmup):
+        net.graph_launch(stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    stats_w = net.sync()
+
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    sampler = ClockSampler(uuid)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    sampler.start()
+    time.sleep(0.3)
+    e_start = torch.cuda.Event(enable_timing=True)
+    e_stop = torch.cuda.Event(enable_timing=True)
+    e_start.record(stream)
+    for k in range(args.steps):
+        evs[k][0].record(stream)
+        net.graph_launch(stream.cuda_stream)
+        evs[k][1].record(stream)
+    e_stop.record(stream)
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    clocks = sampler.stop()
+    stats = net.sync()
+    ms_total = dist.max(e_start.elapsed_time(e_stop))
+    ms_step = ms_total / args.steps
+    kernel_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    seg_steps = S * n_ts
+    value = seg_steps * args.steps * dist.world / (ms_total / 1e3)
+
+    peak, peak_kind = measured_peak_hbm()
+    alg_bytes = BYTES_PER_SEG_STEP * seg_steps
+    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
+    tr = profiled_traffic_per_seg_step()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (tr * seg_steps if tr is not None else None),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "note": "the secant loop is FP64-pipe bound; DRAM traffic is far below the HBM roofline"}
+
+    e2e = None
+    if not args.no_e2e:
+        # public C-ABI path with host buffers: H2D of the step's lateral inflow
+        # from pinned memory inside troute_run, D2H of the routed state
+        qh = qlat_host.numpy()
+        net2 = T.Network(topo, w["params"], cfg=cfg)
+        net2.set_state(w["q0"], w["d0"], w["rl0"])
+        for _ in range(1):
+            net2.run(qh)
+            net2.get_state()
+        torch.cuda.synchronize(dev)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            net2.run(qh)
+            net2.get_state()
+        t1 = time.perf_counter()
+        dist.barrier()
+        e2e_s = dist.max(t1 - t0)
+        e2e = {"value": seg_steps * args.steps * dist.world / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(qh.nbytes), "d2h_bytes_per_step": int((3 * S + R) * 8)}
+        net2.close()
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w)
+    it = stats["iterations"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": {"workload": f"{args.workload}: FP64 MC secant tree routing (plain, single basin), "
+                                   f"{S} segments, {R} reaches, {net.n_levels} levels, {n_ts} steps of "
+                                   f"{w['dt']:.0f} s per bench step, rtol 1e-8 atol 1e-10",
+                       "segments": S, "reaches": R, "levels": net.n_levels, "timesteps_per_step": n_ts,
+                       "l2": "inputs larger than L2 (lateral inflow 3.1 GB read per step)",
+                       "parallelism": "replicas" if dist.world > 1 else "single GPU"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": 2 * args.steps,
+            "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
+                       "early_exits": stats["early_exits"]}}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    net.close()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,228 @@
+/*
+ * troute_gb300 — GB300 (sm_103a) Muskingum-Cunge secant routing, C ABI.
+ *
+ * Drop-in boundary for the t-route MC routing path of
+ * water-prediction/t-route/troute_mc_final.cu (reach-parallel, cpu_mc) and
+ * water-prediction/t-route/wavefront/wavefront_mc.cu (level-scheduled tree,
+ * cpu_wavefront_fp64). Every entry point takes plain pointers and sizes, returns
+ * a status code (TROUTE_OK == 0) and records a message for troute_last_error().
+ * Pointers are host pointers unless the name ends in _device.
+ *
+ * Threading: one troute_handle per host thread; a handle is not re-entrant.
+ * All device-side waits are bounded; a wait that runs out returns
+ * TROUTE_ETIMEOUT and leaves the CUDA context usable.
+ */
+#ifndef TROUTE_GB300_H
+#define TROUTE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum troute_status {
+    TROUTE_OK = 0,
+    TROUTE_EINVAL = 1,   /* bad argument */
+    TROUTE_ETOPO = 2,    /* malformed topology (bad CSR, cycle, reach with two outlets) */
+    TROUTE_ECUDA = 3,    /* CUDA runtime error */
+    TROUTE_ENOMEM = 4,   /* host or device allocation failed */
+    TROUTE_ETIMEOUT = 5, /* a bounded device-side wait ran out */
+    TROUTE_ENODEV = 6,   /* no CUDA device */
+    TROUTE_EIO = 7,      /* file I/O */
+    TROUTE_ESTATE = 8    /* handle unusable (earlier timeout) or checkpoint mismatch */
+};
+
+/* Per-segment channel parameters. Same members, order and size (8 doubles) as
+ * the reference's ChParams, troute_mc_final.cu:26-28, so an array of the
+ * reference's struct can be passed as is. */
+typedef struct troute_chparams {
+    double dx, bw, tw, twcc, n_ch, ncc, cs, s0;
+} troute_chparams;
+
+/* Float parameters as read from params.bin, wavefront_mc.cu:41-44. */
+typedef struct troute_chparams_f32 {
+    float dx, bw, tw, twcc, n_ch, ncc, cs, s0;
+} troute_chparams_f32;
+
+/* Secant and launch configuration. troute_cfg_default() gives the reference's
+ * constants (rtol = atol = 0.01, maxiter 100, 5 attempts,
+ * troute_mc_final.cu:69-74). */
+typedef struct troute_cfg {
+    double rtol;            /* relative depth change that ends the secant loop */
+    double atol;            /* absolute depth change that ends the secant loop */
+    int maxiter;            /* iteration cap of the first attempt (+25 per retry) */
+    int attempts;           /* bracket-widening attempts */
+    int threads_per_block;  /* 0: autotuned / default */
+    int blocks_per_sm;      /* 0: occupancy-derived */
+    long long wait_cycles;  /* bound on each device-side wait, SM clocks; 0: ~2 s */
+    int warm_start;         /* 1: learned warm start (needs troute_set_warm_start) */
+    int warm_k;             /* iterations a warm-started solve gets before the plain solve */
+    int record_history;     /* 1: keep per-step discharge of every segment (troute_get_history) */
+    int reserved[7];
+} troute_cfg;
+
+/* Counters of one run (summed over all segment solves). */
+typedef struct troute_stats {
+    unsigned long long solves;        /* segment solves, including early exits */
+    unsigned long long iterations;    /* secant iterations */
+    unsigned long long retries;       /* solves that needed a widened bracket */
+    unsigned long long early_exits;   /* invalid-parameter or zero-flow solves */
+    unsigned long long warm_used;     /* solves that started from the learned depth */
+    unsigned long long warm_fallback; /* warm-started solves that fell back to the plain secant */
+    unsigned long long iter_hist[16]; /* iterations per solve, last bin = 15+ */
+    double kernel_ms;                 /* device time of the routing kernel(s) */
+    int timeout;                      /* 1 if a bounded wait ran out */
+    int reserved[3];
+} troute_stats;
+
+/* River network in the reference's topo.bin terms (wavefront_mc.cu:577-587,
+ * gen_network.py:12-25). Reaches are listed so that segments of reach r are
+ * reach_seg_start[r] .. +reach_seg_len[r]-1, upstream end first; the upstream
+ * CSR lists for each reach the reaches draining into its head. level_ptr and
+ * level_reach are optional (NULL): the library derives its own schedule. */
+typedef struct troute_topo {
+    int n_reaches;
+    int n_segments;
+    const int* reach_seg_start; /* [n_reaches] */
+    const int* reach_seg_len;   /* [n_reaches] */
+    const int* reach_up_ptr;    /* [n_reaches + 1] */
+    const int* reach_up_idx;    /* [reach_up_ptr[n_reaches]] */
+} troute_topo;
+
+typedef struct troute_handle troute_handle;
+
+/* ---- status ------------------------------------------------------------ */
+const char* troute_last_error(void);
+void troute_cfg_default(troute_cfg* cfg);
+int troute_device_info(int* sm_count, int* cc_major, int* cc_minor, size_t* free_bytes);
+
+/* ---- reach-parallel, one step (replaces cpu_mc, troute_mc_final.cu:167-171,
+ *      and kernel_mc_gpu, :142-148) ------------------------------------- */
+/* Same argument list and meaning as cpu_mc: independent reaches, the first
+ * segment's current inflow seeded by uq, reference tolerances. Host arrays. */
+int troute_mc_reach_parallel(const troute_chparams* p, const double* ql,
+                             const int* rs, const int* rl,
+                             const double* qu, const double* qd, const double* dp,
+                             double* qo, double* vo, double* dpo,
+                             double uq, double dt, int nr);
+/* Same with a configuration and counters (cfg/stats may be NULL). */
+int troute_mc_reach_parallel_cfg(const troute_chparams* p, const double* ql,
+                                 const int* rs, const int* rl,
+                                 const double* qu, const double* qd, const double* dp,
+                                 double* qo, double* vo, double* dpo,
+                                 double uq, double dt, int nr,
+                                 const troute_cfg* cfg, troute_stats* stats);
+/* Device-pointer form of kernel_mc_gpu (all arrays on the device, n_segments
+ * = total segments); asynchronous on `stream` (a cudaStream_t, 0 = default). */
+int troute_mc_reach_parallel_device(const troute_chparams* p, const double* ql,
+                                    const int* rs, const int* rl,
+                                    const double* qu, const double* qd, const double* dp,
+                                    double* qo, double* vo, double* dpo,
+                                    double uq, double dt, int nr, int n_segments,
+                                    const troute_cfg* cfg, void* stream);
+
+/* ---- level-scheduled tree routing, multi-step (replaces
+ *      cpu_wavefront_fp64, wavefront_mc.cu:495-507) ----------------------- */
+/* Exact argument list of cpu_wavefront_fp64 (float inputs, double outputs,
+ * reference tolerances); level_ptr/level_reach are validated against the
+ * topology but the schedule is the library's own. */
+int troute_wavefront_fp64(const troute_chparams_f32* params,
+                          const int* reach_seg_start, const int* reach_seg_len,
+                          const int* reach_up_ptr, const int* reach_up_idx,
+                          const int* level_ptr, const int* level_reach,
+                          int n_reaches, int n_levels, int n_segments,
+                          const float* qlat_ts, const float* qdp0_seg,
+                          const float* dp0_seg, const float* reach_last0,
+                          double* qdc_seg_out_d, double* reach_last_out_d,
+                          int n_timesteps, double dt);
+/* FP64 one-shot tree routing: qlat_ts is [n_ts][n_segments]; outputs are the
+ * final-step discharge, depth, velocity per segment and discharge of each
+ * reach's last segment (any output may be NULL). */
+int troute_route_tree(const troute_topo* topo, const troute_chparams* params,
+                      const double* qlat_ts, const double* qdp0, const double* dp0,
+                      const double* reach_last0, int n_ts, double dt,
+                      const troute_cfg* cfg,
+                      double* q_out, double* d_out, double* v_out,
+                      double* reach_last_out, troute_stats* stats);
+
+/* ---- persistent network handle ---------------------------------------- */
+/* Builds the device schedule and uploads parameters (AoS, user order). */
+int troute_create(troute_handle** h, const troute_topo* topo,
+                  const troute_chparams* params, double dt, const troute_cfg* cfg);
+/* Batched form: n_nets independent networks (basins or ensemble members)
+ * routed together in one persistent launch. params[i] are each network's
+ * parameters. Lateral inflow for the batch is one [n_ts][qlat_cols] matrix:
+ * segment s of network i reads column qlat_col[i][s] (NULL: the next
+ * sum-of-segments column), scaled by qlat_scale[i][s] (NULL: 1). */
+int troute_create_batch(troute_handle** h, int n_nets, const troute_topo* topos,
+                        const troute_chparams* const* params,
+                        const int* const* qlat_col, const double* const* qlat_scale,
+                        int qlat_cols, double dt, const troute_cfg* cfg);
+int troute_destroy(troute_handle* h);
+int troute_set_cfg(troute_handle* h, const troute_cfg* cfg);
+/* Network sizes (any pointer may be NULL). */
+int troute_info(const troute_handle* h, int* n_reaches, int* n_segments, int* n_levels,
+                int* qlat_cols, long long* steps_done);
+/* State in user order over the whole batch (segments then reaches of network
+ * 0, then network 1, ...). NULL reach_last: derived from the last segments. */
+int troute_set_state(troute_handle* h, const double* qdp, const double* dp,
+                     const double* reach_last);
+int troute_get_state(troute_handle* h, double* q, double* d, double* v,
+                     double* reach_last);
+/* Routes n_ts steps; qlat_ts is a host [n_ts][qlat_cols] matrix copied to the
+ * device inside the call. */
+int troute_run(troute_handle* h, const double* qlat_ts, int n_ts, troute_stats* stats);
+/* Same with lateral inflow already on the device ([n_ts][qlat_cols]);
+ * asynchronous on `stream`; call troute_sync for counters and status. */
+int troute_run_device(troute_handle* h, const double* qlat_ts_device, int n_ts, void* stream);
+int troute_sync(troute_handle* h, troute_stats* stats);
+/* Captures `n_ts` steps reading `qlat_ts_device` into a CUDA graph, then
+ * replays it on each troute_graph_launch (state carries over). */
+int troute_graph_capture(troute_handle* h, const double* qlat_ts_device, int n_ts);
+int troute_graph_launch(troute_handle* h, void* stream);
+/* Per-step discharge history [n_ts][n_segments] of the last run (needs
+ * cfg.record_history). */
+int troute_get_history(troute_handle* h, double* q_hist, int n_ts);
+/* Checkpoint of the routing state (q, depth, velocity, reach outflows, step
+ * count). nbytes: in = capacity, out = size; buf NULL queries the size. */
+int troute_checkpoint(troute_handle* h, void* buf, size_t* nbytes);
+int troute_restore(troute_handle* h, const void* buf, size_t nbytes);
+
+/* Launches a one-warp kernel whose wait on a flag nothing sets is bounded by
+ * wait_cycles; returns TROUTE_ETIMEOUT once the wait gives up and the context
+ * stays usable. Exercises the device failure path without faulting. */
+int troute_debug_timeout_probe(long long wait_cycles);
+
+/* ---- schedule and topology helpers ----------------------------------- */
+/* Topological levels as the reference builds them (level 0 = headwater,
+ * level = 1 + max upstream level; gen_network.py:219-231). level_ptr needs
+ * n_reaches + 1 entries of room. */
+int troute_levels(int n_reaches, const int* reach_up_ptr, const int* reach_up_idx,
+                  int* reach_level, int* level_ptr, int* level_reach, int* n_levels);
+/* Checks a topology; returns TROUTE_OK or TROUTE_ETOPO with a message. */
+int troute_validate(const troute_topo* topo);
+
+/* ---- synthetic inputs (seeded, platform-independent) ------------------ */
+/* Uniform random binary river tree (Remy's algorithm) with n_leaves
+ * headwaters -> 2*n_leaves-1 reaches, n_segments segments of 1..max_len per
+ * reach. Arrays: [2n-1], [2n-1], [2n], [2n-2]. */
+int troute_gen_tree(uint64_t seed, int n_leaves, int n_segments, int max_len,
+                    int* reach_seg_start, int* reach_seg_len,
+                    int* reach_up_ptr, int* reach_up_idx);
+/* Channel parameters: dx~U(500,5000), s0~LogU(1e-5,1e-2), n~U(.03,.08),
+ * ncc=2n, bw~U(2,50), tw=3bw, twcc=5tw, cs~U(.5,2). */
+int troute_gen_params(uint64_t seed, int n_segments, troute_chparams* params);
+/* Lateral inflow [n_ts][n_segments] for steps t0..t0+n_ts-1:
+ * Gamma(2, 0.05) m3/s x (1 + 0.5 sin(2 pi t dt / 86400 + phase_s)). */
+int troute_gen_qlat(uint64_t seed, int n_segments, int t0, int n_ts, double dt,
+                    double* qlat);
+/* Ensemble member perturbations: qfac ~ LogN(0, 0.3), nfac ~ U(0.8, 1.2). */
+int troute_gen_member(uint64_t seed, int member, int n_segments, double* qfac,
+                      double* nfac);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

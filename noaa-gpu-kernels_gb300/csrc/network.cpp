@@ -1,0 +1,834 @@
+// Host side of the tree-routing path: topology checks, the device schedule
+// (ALAP levels, level-blocks, segment tiles), the persistent handle and its
+// run / state / checkpoint / graph entry points.
+//
+// Layout in HBM (internal order, built once per handle):
+//   - reaches of one ALAP level are sorted by segment count (longest first)
+//     and cut into level-blocks of 32; internal reach id = block*32 + lane, so
+//     every per-reach array (segment count, upstream CSR row, readiness
+//     counter, outflow ring) is read coalesced by a warp working on a block;
+//   - segment i of lane k of block b lives at tile_off[b] + 32*i + k, so the
+//     warp's loads of "segment i of every reach" are one 256-byte line per
+//     double plane; parameters are six double2 planes (vector loads);
+//   - q, depth, velocity: one double plane each, updated in place each step;
+//   - reach outflow: a [4][reaches] ring indexed by step % 4.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "troute_internal.h"
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+extern "C" const char* troute_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" void troute_cfg_default(troute_cfg* cfg)
+{
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof *cfg);
+    cfg->rtol = 0.01;
+    cfg->atol = 0.01;
+    cfg->maxiter = 100;
+    cfg->attempts = 5;
+    cfg->warm_k = 4;
+}
+
+namespace tr {
+
+int check_cfg(const troute_cfg& c)
+{
+    if (!(c.rtol > 0.0 && c.rtol < 1.0)) return set_error(TROUTE_EINVAL, "cfg.rtol must be in (0, 1)");
+    if (!(c.atol >= 0.0 && c.atol < 1.0)) return set_error(TROUTE_EINVAL, "cfg.atol must be in [0, 1)");
+    if (c.maxiter < 1 || c.maxiter > 100000) return set_error(TROUTE_EINVAL, "cfg.maxiter out of range");
+    if (c.attempts < 1 || c.attempts > 64) return set_error(TROUTE_EINVAL, "cfg.attempts out of range");
+    if (c.threads_per_block != 0 && (c.threads_per_block % 32 != 0 || c.threads_per_block > 128))
+        return set_error(TROUTE_EINVAL, "cfg.threads_per_block must be a multiple of 32, at most 128");
+    if (c.blocks_per_sm < 0 || c.wait_cycles < 0) return set_error(TROUTE_EINVAL, "negative cfg field");
+    return TROUTE_OK;
+}
+
+Tol make_tol(const troute_cfg& c) { return Tol{c.rtol, c.atol, c.maxiter, c.attempts}; }
+
+int cuda_check(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return TROUTE_OK;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return set_error(TROUTE_ENODEV, "%s: %s", what, cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) return set_error(TROUTE_ENOMEM, "%s: %s", what, cudaGetErrorString(e));
+    return set_error(TROUTE_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Topology as the library sees it: a forest over all networks of a handle.
+struct Forest {
+    int R = 0, S = 0;
+    std::vector<int> seg_start, seg_len, up_ptr, up_idx;
+};
+
+// Validates a forest; fills down[] (downstream reach or -1) and a
+// topological order (upstream first).
+int validate_forest(const Forest& f, std::vector<int>& down, std::vector<int>& order)
+{
+    const int R = f.R, S = f.S;
+    if (R < 0 || S < 0) return set_error(TROUTE_ETOPO, "negative sizes");
+    if ((int)f.up_ptr.size() != R + 1 || f.up_ptr[0] != 0)
+        return set_error(TROUTE_ETOPO, "reach_up_ptr must have n_reaches+1 entries starting at 0");
+    for (int r = 0; r < R; ++r)
+        if (f.up_ptr[r + 1] < f.up_ptr[r]) return set_error(TROUTE_ETOPO, "reach_up_ptr not monotone at reach %d", r);
+    if ((size_t)f.up_ptr[R] != f.up_idx.size()) return set_error(TROUTE_ETOPO, "reach_up_idx size mismatch");
+    std::vector<unsigned char> covered((size_t)S, 0);
+    for (int r = 0; r < R; ++r) {
+        const long long a = f.seg_start[r], n = f.seg_len[r];
+        if (n < 0 || a < 0 || a + n > S)
+            return set_error(TROUTE_ETOPO, "reach %d segments [%lld, %lld) outside [0, %d)", r, a, a + n, S);
+        for (long long s = a; s < a + n; ++s) {
+            if (covered[s]) return set_error(TROUTE_ETOPO, "segment %lld belongs to two reaches", s);
+            covered[s] = 1;
+        }
+    }
+    down.assign(R, -1);
+    for (int r = 0; r < R; ++r)
+        for (int k = f.up_ptr[r]; k < f.up_ptr[r + 1]; ++k) {
+            const int u = f.up_idx[k];
+            if (u < 0 || u >= R) return set_error(TROUTE_ETOPO, "upstream index %d of reach %d out of range", u, r);
+            if (u == r) return set_error(TROUTE_ETOPO, "reach %d drains into itself", r);
+            if (down[u] >= 0)
+                return set_error(TROUTE_ETOPO, "reach %d drains into two reaches (%d and %d)", u, down[u], r);
+            down[u] = r;
+        }
+    // Kahn: in-degree = number of upstream reaches
+    std::vector<int> indeg(R);
+    for (int r = 0; r < R; ++r) indeg[r] = f.up_ptr[r + 1] - f.up_ptr[r];
+    order.clear();
+    order.reserve(R);
+    for (int r = 0; r < R; ++r)
+        if (indeg[r] == 0) order.push_back(r);
+    for (size_t i = 0; i < order.size(); ++i) {
+        const int d = down[order[i]];
+        if (d >= 0 && --indeg[d] == 0) order.push_back(d);
+    }
+    if ((int)order.size() != R) return set_error(TROUTE_ETOPO, "topology has a cycle");
+    return TROUTE_OK;
+}
+
+}  // namespace tr
+
+using namespace tr;
+
+// ---------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        if (count <= n && p) return TROUTE_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        if (count == 0) return TROUTE_OK;
+        const int rc = cuda_check(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+        if (rc == TROUTE_OK) n = count;
+        return rc;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct troute_handle {
+    troute_cfg cfg;
+    double dt = 300.0;
+    int R_user = 0, S_user = 0, qlat_cols = 0;
+    int n_levels = 0, n_blocks = 0, R_int = 0;
+    long long S_int = 0;
+    std::vector<int> lb_ptr;           // host copy
+    std::vector<long long> seg_map;    // user segment -> internal slot (-1 none)
+    std::vector<long long> reach_map;  // user reach -> internal reach
+    std::vector<int> user_seg_start, user_seg_len;
+    long long steps_done = 0;
+    bool broken = false;
+
+    DBuf<double2> prm[kParamPlanes];
+    DBuf<int> qcol, nseg, block_level, lb_ptr_d, up_ptr, up_idx, down, done, step_base;
+    DBuf<double> qscale, q, d, v, ring, tmp, qlat_buf, hist;
+    DBuf<long long> tile_off, seg_map_d, reach_map_d;
+    DBuf<unsigned long long> wave_ptr, ticket;
+    DBuf<DevStats> stats;
+    int hist_ts = 0;
+
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int grid = 0, threads = 128;
+    int last_n_ts = 0;
+
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_n_ts = 0;
+
+    NetDev net() const
+    {
+        NetDev n;
+        n.n_blocks = n_blocks;
+        n.n_levels = n_levels;
+        n.n_reach_int = R_int;
+        n.n_seg_int = S_int;
+        for (int i = 0; i < kParamPlanes; ++i) n.prm[i] = prm[i].p;
+        n.qcol = qcol.p;
+        n.qscale = qscale.p;
+        n.nseg = nseg.p;
+        n.tile_off = tile_off.p;
+        n.block_level = block_level.p;
+        n.lb_ptr = lb_ptr_d.p;
+        n.up_ptr = up_ptr.p;
+        n.up_idx = up_idx.p;
+        n.down = down.p;
+        n.q = q.p;
+        n.d = d.p;
+        n.v = v.p;
+        n.ring = ring.p;
+        n.done = done.p;
+        return n;
+    }
+
+    ~troute_handle()
+    {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto& b : prm) b.release();
+        qcol.release(); nseg.release(); block_level.release(); lb_ptr_d.release();
+        up_ptr.release(); up_idx.release(); down.release(); done.release(); step_base.release();
+        qscale.release(); q.release(); d.release(); v.release(); ring.release(); tmp.release();
+        qlat_buf.release(); hist.release(); tile_off.release(); seg_map_d.release();
+        reach_map_d.release(); wave_ptr.release(); ticket.release(); stats.release();
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+template <typename T>
+static int upload(DBuf<T>& b, const std::vector<T>& h, cudaStream_t s)
+{
+    int rc = b.alloc(h.size());
+    if (rc) return rc;
+    if (h.empty()) return TROUTE_OK;
+    return cuda_check(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s),
+                      "upload");
+}
+
+// Builds the device schedule for a forest and uploads everything.
+static int build_handle(troute_handle* H, const Forest& f, const std::vector<troute_chparams>& params,
+                        const std::vector<int>& qcol_user, const std::vector<double>& qscale_user,
+                        bool has_scale)
+{
+    std::vector<int> down, order;
+    int rc = validate_forest(f, down, order);
+    if (rc) return rc;
+    const int R = f.R;
+    H->R_user = R;
+    H->S_user = f.S;
+    H->user_seg_start = f.seg_start;
+    H->user_seg_len = f.seg_len;
+
+    // ALAP level: distance to the outlet, counted down from the deepest level.
+    std::vector<int> dist(R, 0);
+    int maxd = 0;
+    for (int i = R - 1; i >= 0; --i) {
+        const int r = order[i];
+        dist[r] = (down[r] >= 0) ? dist[down[r]] + 1 : 0;
+        maxd = std::max(maxd, dist[r]);
+    }
+    const int L = (R > 0) ? maxd + 1 : 0;
+    H->n_levels = L;
+    std::vector<std::vector<int>> by_level(L);
+    for (int r = 0; r < R; ++r) by_level[L - 1 - dist[r]].push_back(r);
+    std::vector<int> lb_ptr(L + 1, 0), block_level;
+    std::vector<std::vector<int>> blocks;
+    for (int l = 0; l < L; ++l) {
+        auto& v = by_level[l];
+        std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return f.seg_len[a] > f.seg_len[b]; });
+        for (size_t i = 0; i < v.size(); i += kLanes) {
+            blocks.emplace_back(v.begin() + i, v.begin() + std::min(v.size(), i + kLanes));
+            block_level.push_back(l);
+        }
+        lb_ptr[l + 1] = (int)blocks.size();
+    }
+    const int NB = (int)blocks.size();
+    H->n_blocks = NB;
+    H->R_int = NB * kLanes;
+    H->lb_ptr = lb_ptr;
+
+    std::vector<long long> tile_off(NB);
+    long long S_int = 0;
+    H->reach_map.assign(R, -1);
+    H->seg_map.assign(f.S, -1);
+    std::vector<int> nseg(H->R_int, -1);
+    for (int b = 0; b < NB; ++b) {
+        tile_off[b] = S_int;
+        int hmax = 0;
+        for (size_t k = 0; k < blocks[b].size(); ++k) {
+            const int r = blocks[b][k];
+            const int ri = b * kLanes + (int)k;
+            H->reach_map[r] = ri;
+            nseg[ri] = f.seg_len[r];
+            hmax = std::max(hmax, f.seg_len[r]);
+            for (int i = 0; i < f.seg_len[r]; ++i)
+                H->seg_map[f.seg_start[r] + i] = S_int + (long long)i * kLanes + (long long)k;
+        }
+        S_int += (long long)hmax * kLanes;
+    }
+    // one extra slot at the end: the target of segments no reach covers, so
+    // scatter/gather through the segment map never leave the planes
+    const long long trash = S_int;
+    H->S_int = S_int + 1;
+    std::vector<long long> seg_map_dev(H->seg_map);
+    for (auto& m : seg_map_dev)
+        if (m < 0) m = trash;
+
+    // upstream CSR over internal ids, keeping each reach's upstream order
+    // (the order of the floating-point sum at the reach head)
+    std::vector<int> up_ptr(H->R_int + 1, 0), up_idx, down_i(H->R_int, -1);
+    up_idx.reserve(f.up_idx.size());
+    {
+        std::vector<int> user_of(H->R_int, -1);
+        for (int r = 0; r < R; ++r) user_of[H->reach_map[r]] = r;
+        for (int ri = 0; ri < H->R_int; ++ri) {
+            const int r = user_of[ri];
+            if (r >= 0) {
+                for (int k = f.up_ptr[r]; k < f.up_ptr[r + 1]; ++k)
+                    up_idx.push_back((int)H->reach_map[f.up_idx[k]]);
+                if (down[r] >= 0) down_i[ri] = (int)H->reach_map[down[r]];
+            }
+            up_ptr[ri + 1] = (int)up_idx.size();
+        }
+    }
+
+    // parameters in tile order
+    std::vector<double2> planes[kParamPlanes];
+    for (auto& p : planes) p.assign(H->S_int, double2{0.0, 0.0});
+    std::vector<int> qcol(H->S_int, 0);
+    std::vector<double> qscale(has_scale ? H->S_int : 0, 0.0);
+    for (int s = 0; s < f.S; ++s) {
+        const long long t = H->seg_map[s];
+        if (t < 0) continue;
+        const SegP p = derive_seg(params[s]);
+        planes[0][t] = double2{p.dx, p.bw};
+        planes[1][t] = double2{p.twcc, p.n_ch};
+        planes[2][t] = double2{p.ncc, p.s0};
+        planes[3][t] = double2{p.z, p.bfd};
+        planes[4][t] = double2{p.sq_s0, p.sq_1z2};
+        planes[5][t] = double2{p.ck_fac, p.inv_n};
+        qcol[t] = qcol_user[s];
+        if (has_scale) qscale[t] = qscale_user[s];
+    }
+
+    cudaStream_t st = H->stream;
+    for (int i = 0; i < kParamPlanes; ++i)
+        if ((rc = upload(H->prm[i], planes[i], st))) return rc;
+    if ((rc = upload(H->qcol, qcol, st))) return rc;
+    if (has_scale && (rc = upload(H->qscale, qscale, st))) return rc;
+    if ((rc = upload(H->nseg, nseg, st))) return rc;
+    if ((rc = upload(H->tile_off, tile_off, st))) return rc;
+    if ((rc = upload(H->block_level, block_level, st))) return rc;
+    if ((rc = upload(H->lb_ptr_d, lb_ptr, st))) return rc;
+    if ((rc = upload(H->up_ptr, up_ptr, st))) return rc;
+    if ((rc = upload(H->up_idx, up_idx.empty() ? std::vector<int>{0} : up_idx, st))) return rc;
+    if ((rc = upload(H->down, down_i, st))) return rc;
+    if ((rc = upload(H->seg_map_d, seg_map_dev.empty() ? std::vector<long long>{trash} : seg_map_dev, st))) return rc;
+    if ((rc = upload(H->reach_map_d, H->reach_map.empty() ? std::vector<long long>{0} : H->reach_map, st))) return rc;
+    if ((rc = H->q.alloc(H->S_int)) || (rc = H->d.alloc(H->S_int)) || (rc = H->v.alloc(H->S_int))) return rc;
+    if ((rc = H->ring.alloc((size_t)kRing * std::max(1, H->R_int)))) return rc;
+    if ((rc = H->done.alloc(std::max(1, H->R_int))) || (rc = H->step_base.alloc(1))) return rc;
+    if ((rc = H->ticket.alloc(1)) || (rc = H->stats.alloc(1))) return rc;
+    if ((rc = H->tmp.alloc(std::max<size_t>(std::max(H->S_user, H->R_user), 1)))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->q.p, 0, H->S_int * sizeof(double), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->d.p, 0, H->S_int * sizeof(double), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->v.p, 0, H->S_int * sizeof(double), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->ring.p, 0, H->ring.n * sizeof(double), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->done.p, 0, H->done.n * sizeof(int), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->step_base.p, 0, sizeof(int), st), "memset"))) return rc;
+
+    // launch shape: persistent grid, occupancy-sized
+    int dev = 0, sms = 0, bps = 0;
+    if ((rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
+    if ((rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr"))) return rc;
+    H->threads = H->cfg.threads_per_block ? H->cfg.threads_per_block : 128;
+    if ((rc = route_occupancy(H->threads, &bps))) return rc;
+    if (H->cfg.blocks_per_sm > 0) bps = std::min(bps, H->cfg.blocks_per_sm);
+    H->grid = std::max(1, sms * std::max(1, bps));
+    return cuda_check(cudaStreamSynchronize(st), "build sync");
+}
+
+static int new_handle(troute_handle** out, double dt, const troute_cfg* cfg)
+{
+    if (!out) return set_error(TROUTE_EINVAL, "null handle pointer");
+    *out = nullptr;
+    if (!(dt > 0.0)) return set_error(TROUTE_EINVAL, "dt must be positive");
+    troute_cfg c;
+    troute_cfg_default(&c);
+    if (cfg) c = *cfg;
+    int rc = check_cfg(c);
+    if (rc) return rc;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return set_error(TROUTE_ENODEV, "no CUDA device: %s", cudaGetErrorString(e));
+    auto* H = new (std::nothrow) troute_handle();
+    if (!H) return set_error(TROUTE_ENOMEM, "handle allocation");
+    H->cfg = c;
+    H->dt = dt;
+    if ((rc = cuda_check(cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking), "stream"))) { delete H; return rc; }
+    if ((rc = cuda_check(cudaEventCreate(&H->ev0), "event")) || (rc = cuda_check(cudaEventCreate(&H->ev1), "event"))) {
+        delete H;
+        return rc;
+    }
+    *out = H;
+    return TROUTE_OK;
+}
+
+static bool append_topo(Forest& f, const troute_topo& t)
+{
+    if (t.n_reaches < 0 || t.n_segments < 0) return false;
+    if (t.n_reaches > 0 && (!t.reach_seg_start || !t.reach_seg_len || !t.reach_up_ptr)) return false;
+    const int r0 = f.R, s0 = f.S;
+    if (f.up_ptr.empty()) f.up_ptr.push_back(0);
+    const int base = f.up_ptr.back();
+    const int nnz = t.n_reaches > 0 ? t.reach_up_ptr[t.n_reaches] - t.reach_up_ptr[0] : 0;
+    if (nnz < 0 || (nnz > 0 && !t.reach_up_idx)) return false;
+    for (int r = 0; r < t.n_reaches; ++r) {
+        f.seg_start.push_back(t.reach_seg_start[r] + s0);
+        f.seg_len.push_back(t.reach_seg_len[r]);
+        f.up_ptr.push_back(base + t.reach_up_ptr[r + 1] - t.reach_up_ptr[0]);
+    }
+    for (int k = 0; k < nnz; ++k) {
+        const int u = t.reach_up_idx[t.reach_up_ptr[0] + k];
+        f.up_idx.push_back((u >= 0 && u < t.n_reaches) ? u + r0 : -1 - std::abs(u));
+    }
+    f.R += t.n_reaches;
+    f.S += t.n_segments;
+    return true;
+}
+
+extern "C" int troute_create_batch(troute_handle** h, int n_nets, const troute_topo* topos,
+                                   const troute_chparams* const* params,
+                                   const int* const* qlat_col, const double* const* qlat_scale,
+                                   int qlat_cols, double dt, const troute_cfg* cfg)
+{
+    if (n_nets < 1 || !topos || !params) return set_error(TROUTE_EINVAL, "batch needs n_nets >= 1, topos and params");
+    Forest f;
+    f.up_ptr.push_back(0);
+    for (int i = 0; i < n_nets; ++i) {
+        if (!append_topo(f, topos[i])) return set_error(TROUTE_ETOPO, "network %d: malformed topology arrays", i);
+        if (topos[i].n_segments > 0 && !params[i]) return set_error(TROUTE_EINVAL, "network %d: null params", i);
+    }
+    std::vector<troute_chparams> prm;
+    prm.reserve(f.S);
+    std::vector<int> qc;
+    qc.reserve(f.S);
+    std::vector<double> qs;
+    bool has_scale = false;
+    for (int i = 0; i < n_nets; ++i)
+        if (qlat_scale && qlat_scale[i]) has_scale = true;
+    long long col = 0;
+    for (int i = 0; i < n_nets; ++i) {
+        const int S = topos[i].n_segments;
+        for (int s = 0; s < S; ++s) {
+            prm.push_back(params[i][s]);
+            const int c = (qlat_col && qlat_col[i]) ? qlat_col[i][s] : (int)(col + s);
+            qc.push_back(c);
+            if (has_scale) qs.push_back((qlat_scale && qlat_scale[i]) ? qlat_scale[i][s] : 1.0);
+        }
+        col += S;
+    }
+    int cols = qlat_cols > 0 ? qlat_cols : (int)col;
+    for (int c : qc)
+        if (c < 0 || c >= cols) return set_error(TROUTE_EINVAL, "lateral-inflow column %d outside [0, %d)", c, cols);
+    troute_handle* H = nullptr;
+    int rc = new_handle(&H, dt, cfg);
+    if (rc) return rc;
+    H->qlat_cols = cols;
+    rc = build_handle(H, f, prm, qc, qs, has_scale);
+    if (rc) {
+        delete H;
+        return rc;
+    }
+    // default state: zero flow, zero depth
+    *h = H;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_create(troute_handle** h, const troute_topo* topo, const troute_chparams* params,
+                             double dt, const troute_cfg* cfg)
+{
+    if (!topo) return set_error(TROUTE_EINVAL, "null topology");
+    const troute_chparams* p[1] = {params};
+    return troute_create_batch(h, 1, topo, p, nullptr, nullptr, 0, dt, cfg);
+}
+
+extern "C" int troute_destroy(troute_handle* h)
+{
+    delete h;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_set_cfg(troute_handle* h, const troute_cfg* cfg)
+{
+    if (!h || !cfg) return set_error(TROUTE_EINVAL, "null argument");
+    int rc = check_cfg(*cfg);
+    if (rc) return rc;
+    const bool shape = cfg->threads_per_block != h->cfg.threads_per_block || cfg->blocks_per_sm != h->cfg.blocks_per_sm;
+    h->cfg = *cfg;
+    if (shape) {
+        int dev = 0, sms = 0, bps = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        h->threads = cfg->threads_per_block ? cfg->threads_per_block : 128;
+        if ((rc = route_occupancy(h->threads, &bps))) return rc;
+        if (cfg->blocks_per_sm > 0) bps = std::min(bps, cfg->blocks_per_sm);
+        h->grid = std::max(1, sms * std::max(1, bps));
+    }
+    return TROUTE_OK;
+}
+
+extern "C" int troute_info(const troute_handle* h, int* n_reaches, int* n_segments, int* n_levels,
+                           int* qlat_cols, long long* steps_done)
+{
+    if (!h) return set_error(TROUTE_EINVAL, "null handle");
+    if (n_reaches) *n_reaches = h->R_user;
+    if (n_segments) *n_segments = h->S_user;
+    if (n_levels) *n_levels = h->n_levels;
+    if (qlat_cols) *qlat_cols = h->qlat_cols;
+    if (steps_done) *steps_done = h->steps_done;
+    return TROUTE_OK;
+}
+
+// Writes user-order state into the device planes; v may be null (zeroed).
+static int put_state(troute_handle* H, const double* q, const double* dd, const double* v,
+                     const double* reach_last, long long steps)
+{
+    cudaStream_t st = H->stream;
+    int rc;
+    const size_t S = H->S_user, R = H->R_user;
+    if ((rc = cuda_check(cudaMemsetAsync(H->q.p, 0, H->S_int * sizeof(double), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->d.p, 0, H->S_int * sizeof(double), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->v.p, 0, H->S_int * sizeof(double), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->ring.p, 0, H->ring.n * sizeof(double), st), "memset"))) return rc;
+    const double* srcs[3] = {q, dd, v};
+    double* dsts[3] = {H->q.p, H->d.p, H->v.p};
+    for (int i = 0; i < 3; ++i) {
+        if (!srcs[i] || S == 0) continue;
+        if ((rc = cuda_check(cudaMemcpyAsync(H->tmp.p, srcs[i], S * sizeof(double), cudaMemcpyHostToDevice, st), "state upload"))) return rc;
+        if ((rc = launch_scatter(H->tmp.p, H->seg_map_d.p, (long long)S, dsts[i], st))) return rc;
+        if ((rc = cuda_check(cudaStreamSynchronize(st), "state sync"))) return rc;
+    }
+    std::vector<double> rl(R, 0.0);
+    if (reach_last) {
+        std::memcpy(rl.data(), reach_last, R * sizeof(double));
+    } else if (q) {
+        // outflow of the previous step = discharge of the reach's last segment
+        // (wavefront_mc.cu:675-680); a reach without segments sends nothing
+        for (size_t r = 0; r < R; ++r)
+            rl[r] = H->user_seg_len[r] > 0 ? q[H->user_seg_start[r] + H->user_seg_len[r] - 1] : 0.0;
+    }
+    const int slot = (int)(((steps - 1) % kRing + kRing) % kRing);
+    if (R > 0) {
+        if ((rc = cuda_check(cudaMemcpyAsync(H->tmp.p, rl.data(), R * sizeof(double), cudaMemcpyHostToDevice, st), "state upload"))) return rc;
+        if ((rc = launch_scatter(H->tmp.p, H->reach_map_d.p, (long long)R, H->ring.p + (size_t)slot * H->R_int, st))) return rc;
+    }
+    if ((rc = launch_fill_int(H->done.p, H->R_int, nullptr, (int)steps, st))) return rc;
+    if ((rc = launch_fill_int(H->step_base.p, 1, nullptr, (int)steps, st))) return rc;
+    if ((rc = cuda_check(cudaStreamSynchronize(st), "state sync"))) return rc;
+    H->steps_done = steps;
+    H->broken = false;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_set_state(troute_handle* h, const double* qdp, const double* dp,
+                                const double* reach_last)
+{
+    if (!h) return set_error(TROUTE_EINVAL, "null handle");
+    return put_state(h, qdp, dp, nullptr, reach_last, 0);
+}
+
+extern "C" int troute_get_state(troute_handle* h, double* q, double* d, double* v, double* reach_last)
+{
+    if (!h) return set_error(TROUTE_EINVAL, "null handle");
+    cudaStream_t st = h->stream;
+    int rc;
+    const size_t S = h->S_user, R = h->R_user;
+    const double* srcs[3] = {h->q.p, h->d.p, h->v.p};
+    double* dsts[3] = {q, d, v};
+    // segments not covered by any reach carry zeros
+    for (int i = 0; i < 3; ++i) {
+        if (!dsts[i] || S == 0) continue;
+        if ((rc = launch_gather(srcs[i], h->seg_map_d.p, (long long)S, h->tmp.p, st))) return rc;
+        if ((rc = cuda_check(cudaMemcpyAsync(dsts[i], h->tmp.p, S * sizeof(double), cudaMemcpyDeviceToHost, st), "state download"))) return rc;
+        if ((rc = cuda_check(cudaStreamSynchronize(st), "state sync"))) return rc;
+        for (size_t s = 0; s < S; ++s)
+            if (h->seg_map[s] < 0) dsts[i][s] = 0.0;
+    }
+    if (reach_last && R > 0) {
+        const int slot = (int)(((h->steps_done - 1) % kRing + kRing) % kRing);
+        if ((rc = launch_gather(h->ring.p + (size_t)slot * h->R_int, h->reach_map_d.p, (long long)R, h->tmp.p, st))) return rc;
+        if ((rc = cuda_check(cudaMemcpyAsync(reach_last, h->tmp.p, R * sizeof(double), cudaMemcpyDeviceToHost, st), "state download"))) return rc;
+        if ((rc = cuda_check(cudaStreamSynchronize(st), "state sync"))) return rc;
+    }
+    return TROUTE_OK;
+}
+
+// Ticket prefix per wave for a run of n_ts steps: wave w holds the blocks of
+// levels max(0, w-n_ts+1) .. min(L-1, w), each at step w - level.
+static void wave_prefix(const std::vector<int>& lb_ptr, int L, int n_ts, std::vector<unsigned long long>& wp)
+{
+    const int W = n_ts + L - 1;
+    wp.assign(W + 1, 0);
+    for (int w = 0; w < W; ++w) {
+        const int lo = std::max(0, w - n_ts + 1), hi = std::min(L - 1, w);
+        const unsigned long long c = hi >= lo ? (unsigned long long)(lb_ptr[hi + 1] - lb_ptr[lo]) : 0ull;
+        wp[w + 1] = wp[w] + c;
+    }
+}
+
+// Enqueues one run (wave table already on the device) on stream `st`.
+static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, cudaStream_t st, bool timed)
+{
+    int rc;
+    RunDev run;
+    run.step_base = H->step_base.p;
+    run.n_ts = n_ts;
+    run.dt = H->dt;
+    run.qlat = qlat_dev;
+    run.qlat_ld = H->qlat_cols;
+    run.wave_ptr = H->wave_ptr.p;
+    run.n_waves = n_ts + H->n_levels - 1;
+    std::vector<unsigned long long> wp;
+    wave_prefix(H->lb_ptr, H->n_levels, n_ts, wp);
+    run.n_tickets = wp.back();
+    run.ticket = H->ticket.p;
+    run.stats = H->stats.p;
+    run.wait_cycles = H->cfg.wait_cycles > 0 ? H->cfg.wait_cycles : 4000000000LL;
+    run.tol = make_tol(H->cfg);
+    run.q_hist = (H->cfg.record_history && H->hist.p) ? H->hist.p : nullptr;
+    if ((rc = cuda_check(cudaMemsetAsync(H->ticket.p, 0, sizeof(unsigned long long), st), "memset"))) return rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->stats.p, 0, sizeof(DevStats), st), "memset"))) return rc;
+    if (timed && (rc = cuda_check(cudaEventRecord(H->ev0, st), "event"))) return rc;
+    if ((rc = launch_route(H->net(), run, H->grid, H->threads, st))) return rc;
+    if (timed && (rc = cuda_check(cudaEventRecord(H->ev1, st), "event"))) return rc;
+    return launch_bump_steps(H->step_base.p, n_ts, st);
+}
+
+static int prepare_run(troute_handle* H, int n_ts)
+{
+    int rc;
+    std::vector<unsigned long long> wp;
+    wave_prefix(H->lb_ptr, H->n_levels, n_ts, wp);
+    if ((rc = H->wave_ptr.alloc(wp.size()))) return rc;
+    if ((rc = cuda_check(cudaMemcpyAsync(H->wave_ptr.p, wp.data(), wp.size() * sizeof(unsigned long long),
+                                         cudaMemcpyHostToDevice, H->stream), "wave upload")))
+        return rc;
+    if (H->cfg.record_history) {
+        if ((rc = H->hist.alloc((size_t)n_ts * H->S_int))) return rc;
+        H->hist_ts = n_ts;
+    }
+    return cuda_check(cudaStreamSynchronize(H->stream), "wave sync");
+}
+
+static int collect(troute_handle* H, troute_stats* stats, bool timed)
+{
+    DevStats ds;
+    int rc = cuda_check(cudaMemcpy(&ds, H->stats.p, sizeof ds, cudaMemcpyDeviceToHost), "stats download");
+    if (rc) return rc;
+    if (stats) {
+        std::memset(stats, 0, sizeof *stats);
+        stats->solves = ds.solves;
+        stats->iterations = ds.iterations;
+        stats->retries = ds.retries;
+        stats->early_exits = ds.early_exits;
+        stats->warm_used = ds.warm_used;
+        stats->warm_fallback = ds.warm_fallback;
+        for (int i = 0; i < 16; ++i) stats->iter_hist[i] = ds.hist[i];
+        stats->timeout = ds.error == TROUTE_ETIMEOUT;
+        if (timed) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, H->ev0, H->ev1);
+            stats->kernel_ms = ms;
+        }
+    }
+    if (ds.error == TROUTE_ETIMEOUT) {
+        H->broken = true;
+        return set_error(TROUTE_ETIMEOUT, "device wait ran out (internal reach %d, step %d, wait kind %d)",
+                         ds.err_reach, ds.err_step, ds.err_where);
+    }
+    if (ds.error) {
+        H->broken = true;
+        return set_error(ds.error, "device reported error %d", ds.error);
+    }
+    return TROUTE_OK;
+}
+
+extern "C" int troute_run_device(troute_handle* h, const double* qlat_ts_device, int n_ts, void* stream)
+{
+    if (!h) return set_error(TROUTE_EINVAL, "null handle");
+    if (h->broken) return set_error(TROUTE_ESTATE, "handle unusable after an earlier device failure; restore or set state");
+    if (n_ts < 0) return set_error(TROUTE_EINVAL, "n_ts < 0");
+    if (n_ts == 0 || h->R_user == 0) return TROUTE_OK;
+    if (!qlat_ts_device) return set_error(TROUTE_EINVAL, "null lateral inflow");
+    int rc = prepare_run(h, n_ts);
+    if (rc) return rc;
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+    if (stream) {
+        // order our stream's prior work (uploads) before the caller's stream
+        cudaEvent_t e;
+        cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        cudaEventRecord(e, h->stream);
+        cudaStreamWaitEvent(st, e, 0);
+        cudaEventDestroy(e);
+    }
+    if ((rc = enqueue_run(h, qlat_ts_device, n_ts, st, true))) return rc;
+    h->steps_done += n_ts;
+    h->last_n_ts = n_ts;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_sync(troute_handle* h, troute_stats* stats)
+{
+    if (!h) return set_error(TROUTE_EINVAL, "null handle");
+    int rc = cuda_check(cudaDeviceSynchronize(), "run");
+    if (rc) return rc;
+    return collect(h, stats, h->last_n_ts > 0);
+}
+
+extern "C" int troute_run(troute_handle* h, const double* qlat_ts, int n_ts, troute_stats* stats)
+{
+    if (!h) return set_error(TROUTE_EINVAL, "null handle");
+    if (h->broken) return set_error(TROUTE_ESTATE, "handle unusable after an earlier device failure; restore or set state");
+    if (n_ts < 0) return set_error(TROUTE_EINVAL, "n_ts < 0");
+    if (stats) std::memset(stats, 0, sizeof *stats);
+    if (n_ts == 0 || h->R_user == 0) return TROUTE_OK;
+    if (!qlat_ts) return set_error(TROUTE_EINVAL, "null lateral inflow");
+    const size_t n = (size_t)n_ts * (size_t)h->qlat_cols;
+    int rc = h->qlat_buf.alloc(std::max<size_t>(n, 1));
+    if (rc) return rc;
+    if ((rc = cuda_check(cudaMemcpyAsync(h->qlat_buf.p, qlat_ts, n * sizeof(double), cudaMemcpyHostToDevice, h->stream),
+                         "qlat upload")))
+        return rc;
+    if ((rc = troute_run_device(h, h->qlat_buf.p, n_ts, nullptr))) return rc;
+    rc = cuda_check(cudaStreamSynchronize(h->stream), "run");
+    if (rc) return rc;
+    return collect(h, stats, true);
+}
+
+extern "C" int troute_graph_capture(troute_handle* h, const double* qlat_ts_device, int n_ts)
+{
+    if (!h || !qlat_ts_device || n_ts <= 0) return set_error(TROUTE_EINVAL, "bad graph arguments");
+    int rc = prepare_run(h, n_ts);
+    if (rc) return rc;
+    if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+    if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+    if ((rc = cuda_check(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"))) return rc;
+    rc = enqueue_run(h, qlat_ts_device, n_ts, h->stream, false);
+    cudaGraph_t g = nullptr;
+    const int rc2 = cuda_check(cudaStreamEndCapture(h->stream, &g), "end capture");
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (rc2) return rc2;
+    h->graph = g;
+    if ((rc = cuda_check(cudaGraphInstantiate(&h->graph_exec, g, 0), "graph instantiate"))) return rc;
+    h->graph_n_ts = n_ts;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_graph_launch(troute_handle* h, void* stream)
+{
+    if (!h || !h->graph_exec) return set_error(TROUTE_EINVAL, "no captured graph");
+    if (h->broken) return set_error(TROUTE_ESTATE, "handle unusable after an earlier device failure");
+    int rc = cuda_check(cudaGraphLaunch(h->graph_exec, stream ? (cudaStream_t)stream : h->stream), "graph launch");
+    if (rc) return rc;
+    h->steps_done += h->graph_n_ts;
+    h->last_n_ts = 0;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_get_history(troute_handle* h, double* q_hist, int n_ts)
+{
+    if (!h || !q_hist) return set_error(TROUTE_EINVAL, "null argument");
+    if (!h->cfg.record_history || !h->hist.p || n_ts != h->hist_ts)
+        return set_error(TROUTE_ESTATE, "no history of %d steps recorded (set cfg.record_history)", n_ts);
+    const size_t S = h->S_user;
+    int rc;
+    for (int t = 0; t < n_ts; ++t) {
+        if ((rc = launch_gather(h->hist.p + (size_t)t * h->S_int, h->seg_map_d.p, (long long)S, h->tmp.p, h->stream))) return rc;
+        if ((rc = cuda_check(cudaMemcpyAsync(q_hist + (size_t)t * S, h->tmp.p, S * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "history download"))) return rc;
+    }
+    return cuda_check(cudaStreamSynchronize(h->stream), "history sync");
+}
+
+// checkpoint: header + q, d, v [S_user] + reach_last [R_user], user order
+struct CkptHeader {
+    char magic[8];
+    int version, R, S, pad;
+    long long steps;
+};
+
+extern "C" int troute_checkpoint(troute_handle* h, void* buf, size_t* nbytes)
+{
+    if (!h || !nbytes) return set_error(TROUTE_EINVAL, "null argument");
+    const size_t need = sizeof(CkptHeader) + (3 * (size_t)h->S_user + (size_t)h->R_user) * sizeof(double);
+    if (!buf) { *nbytes = need; return TROUTE_OK; }
+    if (*nbytes < need) { *nbytes = need; return set_error(TROUTE_EINVAL, "checkpoint buffer too small"); }
+    if (h->broken) return set_error(TROUTE_ESTATE, "handle state invalid after a device failure");
+    CkptHeader hd;
+    std::memset(&hd, 0, sizeof hd);
+    std::memcpy(hd.magic, "TRGB300", 8);
+    hd.version = 1;
+    hd.R = h->R_user;
+    hd.S = h->S_user;
+    hd.steps = h->steps_done;
+    char* p = static_cast<char*>(buf);
+    std::memcpy(p, &hd, sizeof hd);
+    double* x = reinterpret_cast<double*>(p + sizeof hd);
+    const size_t S = h->S_user;
+    int rc = troute_get_state(h, x, x + S, x + 2 * S, x + 3 * S);
+    if (rc) return rc;
+    *nbytes = need;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_restore(troute_handle* h, const void* buf, size_t nbytes)
+{
+    if (!h || !buf) return set_error(TROUTE_EINVAL, "null argument");
+    CkptHeader hd;
+    if (nbytes < sizeof hd) return set_error(TROUTE_ESTATE, "checkpoint truncated");
+    std::memcpy(&hd, buf, sizeof hd);
+    if (std::memcmp(hd.magic, "TRGB300", 8) != 0 || hd.version != 1) return set_error(TROUTE_ESTATE, "not a checkpoint");
+    if (hd.R != h->R_user || hd.S != h->S_user) return set_error(TROUTE_ESTATE, "checkpoint is for another network");
+    const size_t S = h->S_user;
+    if (nbytes < sizeof hd + (3 * S + (size_t)hd.R) * sizeof(double)) return set_error(TROUTE_ESTATE, "checkpoint truncated");
+    std::vector<double> x(3 * S + hd.R);
+    std::memcpy(x.data(), static_cast<const char*>(buf) + sizeof hd, x.size() * sizeof(double));
+    return put_state(h, x.data(), x.data() + S, x.data() + 2 * S, x.data() + 3 * S, hd.steps);
+}

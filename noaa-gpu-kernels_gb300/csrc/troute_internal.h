@@ -1,0 +1,133 @@
+// Internal declarations shared by the host (C++) and device (CUDA) halves of
+// libtroute_gb300.so. Nothing here is part of the public C ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cmath>
+
+#include <vector_types.h>
+
+#include "../../include/troute_gb300.h"
+
+#if defined(__CUDACC__)
+#define TR_HD __host__ __device__
+#else
+#define TR_HD
+#endif
+
+// Records a message for troute_last_error() and returns `code`.
+int set_error(int code, const char* fmt, ...);
+
+namespace tr {
+
+uint64_t hash3(uint64_t seed, uint64_t stream, uint64_t ctr);
+double u01(uint64_t h);
+double det_log(double x);
+double det_exp(double x);
+double det_sin(double x);
+
+constexpr int kLanes = 32;      // reaches per level-block (one warp)
+constexpr int kRing = 4;        // depth of the per-reach outflow ring (steps)
+constexpr double kMinDepth = 0.01;  // troute_mc_final.cu:58
+
+// Secant tolerances handed to the device.
+struct Tol {
+    double rtol, atol;
+    int maxiter, attempts;
+};
+
+// Per-segment values the solver reads, derived once from ChParams on the host
+// with the same IEEE operations the reference performs per solve
+// (troute_mc_final.cu:181-183), stored as six double2 planes.
+//   p[0] = {dx, bw}        p[1] = {twcc, n_ch}      p[2] = {ncc, s0}
+//   p[3] = {z, bfd}        p[4] = {sqrt(s0), sqrt(1+z^2)}
+//   p[5] = {sqrt(s0)/n_ch, 1/n_ch}
+constexpr int kParamPlanes = 6;
+
+struct SegP {
+    double dx, bw, twcc, n_ch, ncc, s0, z, bfd, sq_s0, sq_1z2, ck_fac, inv_n;
+};
+
+// Derived values from the reference's parameter record, :181-183.
+TR_HD inline SegP derive_seg(const troute_chparams& c)
+{
+    SegP p;
+    p.dx = c.dx; p.bw = c.bw; p.twcc = c.twcc; p.n_ch = c.n_ch; p.ncc = c.ncc; p.s0 = c.s0;
+    p.z = (c.cs == 0.0) ? 1.0 : 1.0 / c.cs;
+    p.bfd = (c.bw > c.tw) ? c.bw / 0.00001 : (c.bw == c.tw) ? c.bw / (2.0 * p.z) : (c.tw - c.bw) / (2.0 * p.z);
+    p.sq_s0 = sqrt(c.s0);
+    p.sq_1z2 = sqrt(1.0 + p.z * p.z);
+    p.ck_fac = p.sq_s0 / c.n_ch;
+    p.inv_n = 1.0 / c.n_ch;
+    return p;
+}
+
+// Device counters of one run.
+struct DevStats {
+    unsigned long long solves, iterations, retries, early_exits, warm_used, warm_fallback;
+    unsigned long long hist[16];
+    int error;       // 0 ok, TROUTE_ETIMEOUT, TROUTE_EINVAL (bad index seen)
+    int err_reach;   // internal reach of the first failure
+    int err_step;    // step of the first failure
+    int err_where;   // 1 own, 2 upstream, 3 downstream back-pressure, 4 bounds
+};
+
+// Static network description on the device (internal order).
+struct NetDev {
+    int n_blocks;            // level-blocks of kLanes reaches
+    int n_levels;            // ALAP levels
+    int n_reach_int;         // n_blocks * kLanes
+    long long n_seg_int;     // padded tile storage
+    const double2* prm[kParamPlanes];  // [n_seg_int] each
+    const int* qcol;         // [n_seg_int] lateral-inflow column of each segment
+    const double* qscale;    // [n_seg_int] or null
+    const int* nseg;         // [n_reach_int], -1 for padding lanes
+    const long long* tile_off;  // [n_blocks] first segment slot of a block
+    const int* block_level;  // [n_blocks]
+    const int* lb_ptr;       // [n_levels + 1] blocks of each level
+    const int* up_ptr;       // [n_reach_int + 1]
+    const int* up_idx;       // internal reach ids
+    const int* down;         // [n_reach_int] internal id or -1
+    // mutable state
+    double* q;               // [n_seg_int] discharge of the last completed step
+    double* d;               // depth
+    double* v;               // velocity
+    double* ring;            // [kRing][n_reach_int] outflow of each reach per step
+    int* done;               // [n_reach_int] cumulative completed steps
+};
+
+// One routing run (n_ts steps).
+struct RunDev {
+    const int* step_base;    // device: cumulative steps before this run
+    int n_ts;
+    double dt;
+    const double* qlat;      // [n_ts][qlat_ld]
+    long long qlat_ld;
+    const unsigned long long* wave_ptr;  // [n_ts + n_levels] ticket prefix per wave
+    int n_waves;
+    unsigned long long n_tickets;
+    unsigned long long* ticket;  // device counter
+    DevStats* stats;
+    long long wait_cycles;
+    Tol tol;
+    double* q_hist;          // optional [n_ts][n_seg_int]
+};
+
+// Launch helpers implemented in kernels.cu (all asynchronous on `stream`).
+int launch_reach_parallel(const troute_chparams* p, const double* ql, const int* rs,
+                          const int* rl, const double* qu, const double* qd, const double* dp,
+                          double* qo, double* vo, double* dpo, double uq, double dt, int nr,
+                          int n_segments, const Tol& tol, DevStats* stats, int threads,
+                          void* stream);
+int launch_route(const NetDev& net, const RunDev& run, int grid, int threads, void* stream);
+int route_occupancy(int threads, int* blocks_per_sm);
+int launch_bump_steps(int* step_base, int n_ts, void* stream);
+int launch_fill_int(int* p, long long n, const int* value_dev, int value_host, void* stream);
+int launch_scatter(const double* src, const long long* map, long long n, double* dst,
+                   void* stream);
+int launch_gather(const double* src, const long long* map, long long n, double* dst,
+                  void* stream);
+int launch_timeout_probe(DevStats* stats, long long wait_cycles, void* stream);
+
+}  // namespace tr

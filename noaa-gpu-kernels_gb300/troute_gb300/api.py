@@ -1,0 +1,421 @@
+"""Python mirror of the t-route MC routing interface over libtroute_gb300.so.
+
+Function names and argument meaning follow the reference's entry points:
+  mc_reach_parallel  <- cpu_mc / kernel_mc_gpu
+                        (water-prediction/t-route/troute_mc_final.cu:142-171)
+  wavefront_fp64     <- cpu_wavefront_fp64
+                        (water-prediction/t-route/wavefront/wavefront_mc.cu:495-507)
+  route_tree / Network  FP64 multi-step tree routing with persistent state.
+Every call goes through the C ABI declared in include/troute_gb300.h; a
+non-zero status raises TrouteError with the library's message. The CUDA
+library must have been built (troute_gb300.build.build()); there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+# ---------------------------------------------------------------------------
+# library loading
+# ---------------------------------------------------------------------------
+_LIB = None
+
+
+class TrouteError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"troute error {code}: {msg}")
+        self.code = code
+
+
+OK, EINVAL, ETOPO, ECUDA, ENOMEM, ETIMEOUT, ENODEV, EIO, ESTATE = range(9)
+
+
+class ChParams(C.Structure):
+    """Same layout as the reference's ChParams (troute_mc_final.cu:26-28)."""
+
+    _fields_ = [(n, C.c_double) for n in ("dx", "bw", "tw", "twcc", "n_ch", "ncc", "cs", "s0")]
+
+
+CHPARAMS_DTYPE = np.dtype([(n, "<f8") for n in ("dx", "bw", "tw", "twcc", "n_ch", "ncc", "cs", "s0")])
+CHPARAMS_F32_DTYPE = np.dtype([(n, "<f4") for n in ("dx", "bw", "tw", "twcc", "n_ch", "ncc", "cs", "s0")])
+
+
+class Cfg(C.Structure):
+    _fields_ = [
+        ("rtol", C.c_double),
+        ("atol", C.c_double),
+        ("maxiter", C.c_int),
+        ("attempts", C.c_int),
+        ("threads_per_block", C.c_int),
+        ("blocks_per_sm", C.c_int),
+        ("wait_cycles", C.c_longlong),
+        ("warm_start", C.c_int),
+        ("warm_k", C.c_int),
+        ("record_history", C.c_int),
+        ("reserved", C.c_int * 7),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("solves", C.c_ulonglong),
+        ("iterations", C.c_ulonglong),
+        ("retries", C.c_ulonglong),
+        ("early_exits", C.c_ulonglong),
+        ("warm_used", C.c_ulonglong),
+        ("warm_fallback", C.c_ulonglong),
+        ("iter_hist", C.c_ulonglong * 16),
+        ("kernel_ms", C.c_double),
+        ("timeout", C.c_int),
+        ("reserved", C.c_int * 3),
+    ]
+
+    def as_dict(self) -> dict:
+        return {
+            "solves": int(self.solves),
+            "iterations": int(self.iterations),
+            "retries": int(self.retries),
+            "early_exits": int(self.early_exits),
+            "warm_used": int(self.warm_used),
+            "warm_fallback": int(self.warm_fallback),
+            "iter_hist": [int(x) for x in self.iter_hist],
+            "kernel_ms": float(self.kernel_ms),
+            "timeout": int(self.timeout),
+        }
+
+
+class Topo(C.Structure):
+    _fields_ = [
+        ("n_reaches", C.c_int),
+        ("n_segments", C.c_int),
+        ("reach_seg_start", C.POINTER(C.c_int)),
+        ("reach_seg_len", C.POINTER(C.c_int)),
+        ("reach_up_ptr", C.POINTER(C.c_int)),
+        ("reach_up_idx", C.POINTER(C.c_int)),
+    ]
+
+
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+_U64 = C.c_uint64
+
+# name -> argtypes (restype is int unless noted)
+_SIGS = {
+    "troute_last_error": ([], C.c_char_p),
+    "troute_cfg_default": ([_P], None),
+    "troute_device_info": ([_P, _P, _P, _P], _I),
+    "troute_mc_reach_parallel": ([_P] * 10 + [_D, _D, _I], _I),
+    "troute_mc_reach_parallel_cfg": ([_P] * 10 + [_D, _D, _I, _P, _P], _I),
+    "troute_mc_reach_parallel_device": ([_P] * 10 + [_D, _D, _I, _I, _P, _P], _I),
+    "troute_wavefront_fp64": ([_P] * 7 + [_I, _I, _I] + [_P] * 6 + [_I, _D], _I),
+    "troute_route_tree": ([_P] * 6 + [_I, _D, _P] + [_P] * 5, _I),
+    "troute_create": ([_P, _P, _P, _D, _P], _I),
+    "troute_create_batch": ([_P, _I, _P, _P, _P, _P, _I, _D, _P], _I),
+    "troute_destroy": ([_P], _I),
+    "troute_set_cfg": ([_P, _P], _I),
+    "troute_info": ([_P, _P, _P, _P, _P, _P], _I),
+    "troute_set_state": ([_P, _P, _P, _P], _I),
+    "troute_get_state": ([_P, _P, _P, _P, _P], _I),
+    "troute_run": ([_P, _P, _I, _P], _I),
+    "troute_run_device": ([_P, _P, _I, _P], _I),
+    "troute_sync": ([_P, _P], _I),
+    "troute_graph_capture": ([_P, _P, _I], _I),
+    "troute_graph_launch": ([_P, _P], _I),
+    "troute_get_history": ([_P, _P, _I], _I),
+    "troute_checkpoint": ([_P, _P, _P], _I),
+    "troute_restore": ([_P, _P, C.c_size_t], _I),
+    "troute_debug_timeout_probe": ([C.c_longlong], _I),
+    "troute_levels": ([_I, _P, _P, _P, _P, _P, _P], _I),
+    "troute_validate": ([_P], _I),
+    "troute_gen_tree": ([_U64, _I, _I, _I, _P, _P, _P, _P], _I),
+    "troute_gen_params": ([_U64, _I, _P], _I),
+    "troute_gen_qlat": ([_U64, _I, _I, _I, _D, _P], _I),
+    "troute_gen_member": ([_U64, _I, _I, _P, _P], _I),
+}
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Loads libtroute_gb300.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise ImportError(f"{path} is missing: build it with troute_gb300.build.build()")
+        L = C.CDLL(path)
+        for name, (argt, rest) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = argt
+            fn.restype = rest
+        _LIB = L
+    return _LIB
+
+
+def exported_symbols() -> list:
+    return list(_SIGS)
+
+
+def _check(rc: int):
+    if rc != OK:
+        raise TrouteError(rc, lib().troute_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _params(p):
+    p = np.ascontiguousarray(p)
+    if p.dtype == CHPARAMS_DTYPE:
+        return p
+    if p.dtype.names is not None:
+        return np.ascontiguousarray(p.astype(CHPARAMS_DTYPE))
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    if p.ndim != 2 or p.shape[1] != 8:
+        raise ValueError("params must be a ChParams record array or an (n, 8) float array")
+    return p.view(CHPARAMS_DTYPE).reshape(-1)
+
+
+def make_cfg(rtol=0.01, atol=0.01, maxiter=100, attempts=5, **kw) -> Cfg:
+    c = Cfg()
+    lib().troute_cfg_default(C.byref(c))
+    c.rtol, c.atol, c.maxiter, c.attempts = rtol, atol, maxiter, attempts
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def timeout_probe(wait_cycles: int = 2_000_000) -> int:
+    """Runs the bounded-wait probe kernel; returns the status code (ETIMEOUT expected)."""
+    return lib().troute_debug_timeout_probe(int(wait_cycles))
+
+
+def device_info() -> dict:
+    sm, ma, mi, fr = _I(), _I(), _I(), C.c_size_t()
+    _check(lib().troute_device_info(C.byref(sm), C.byref(ma), C.byref(mi), C.byref(fr)))
+    return {"sm_count": sm.value, "cc": (ma.value, mi.value), "free_bytes": fr.value}
+
+
+# ---------------------------------------------------------------------------
+# reach-parallel (cpu_mc)
+# ---------------------------------------------------------------------------
+def mc_reach_parallel(p, ql, rs, rl, qu, qd, dp, uq: float = 10.0, dt: float = 300.0, cfg: Cfg | None = None,
+                      return_stats: bool = False):
+    """cpu_mc on the GPU: returns (qo, vo, dpo) (+ stats dict)."""
+    p = _params(p)
+    n = p.shape[0]
+    ql, qu, qd, dp = (_f64(x, n) for x in (ql, qu, qd, dp))
+    rs, rl = _i32(rs), _i32(rl)
+    qo, vo, dpo = np.zeros(n), np.zeros(n), np.zeros(n)
+    st = Stats()
+    _check(lib().troute_mc_reach_parallel_cfg(
+        _ptr(p), _ptr(ql), _ptr(rs), _ptr(rl), _ptr(qu), _ptr(qd), _ptr(dp), _ptr(qo), _ptr(vo), _ptr(dpo),
+        float(uq), float(dt), int(rs.size), C.byref(cfg) if cfg is not None else None, C.byref(st)))
+    return (qo, vo, dpo, st.as_dict()) if return_stats else (qo, vo, dpo)
+
+
+# ---------------------------------------------------------------------------
+# topology helpers
+# ---------------------------------------------------------------------------
+def _topo_struct(seg_start, seg_len, up_ptr, up_idx, n_segments):
+    arrs = [_i32(seg_start), _i32(seg_len), _i32(up_ptr), _i32(up_idx if len(up_idx) else np.zeros(1, np.int32))]
+    t = Topo()
+    t.n_reaches = int(arrs[0].size)
+    t.n_segments = int(n_segments)
+    t.reach_seg_start, t.reach_seg_len, t.reach_up_ptr, t.reach_up_idx = (
+        a.ctypes.data_as(C.POINTER(C.c_int)) for a in arrs)
+    return t, arrs
+
+
+def levels(up_ptr, up_idx):
+    """Reference-style levels (gen_network.py:219-231): (reach_level, level_ptr, level_reach)."""
+    up_ptr, up_idx = _i32(up_ptr), _i32(up_idx if len(up_idx) else np.zeros(1, np.int32))
+    R = up_ptr.size - 1
+    lv = np.zeros(max(R, 1), np.int32)
+    lp = np.zeros(R + 1, np.int32)
+    lr = np.zeros(max(R, 1), np.int32)
+    nl = _I()
+    _check(lib().troute_levels(R, _ptr(up_ptr), _ptr(up_idx), _ptr(lv), _ptr(lp), _ptr(lr), C.byref(nl)))
+    return lv[:R], lp[: nl.value + 1], lr[:R]
+
+
+def validate(seg_start, seg_len, up_ptr, up_idx, n_segments):
+    t, _keep = _topo_struct(seg_start, seg_len, up_ptr, up_idx, n_segments)
+    _check(lib().troute_validate(C.byref(t)))
+
+
+# ---------------------------------------------------------------------------
+# tree routing
+# ---------------------------------------------------------------------------
+def wavefront_fp64(params_f32, seg_start, seg_len, up_ptr, up_idx, level_ptr, level_reach, qlat_ts_f32,
+                   qdp0_f32, dp0_f32, reach_last0_f32, n_timesteps: int, dt: float = 300.0):
+    """cpu_wavefront_fp64 drop-in: float inputs, (q_final, reach_last_final) doubles."""
+    p = np.ascontiguousarray(params_f32)
+    if p.dtype != CHPARAMS_F32_DTYPE:
+        p = np.ascontiguousarray(np.asarray(p, np.float32).reshape(-1, 8)).view(CHPARAMS_F32_DTYPE).reshape(-1)
+    S, R = p.shape[0], len(seg_start)
+    ints = [_i32(x) for x in (seg_start, seg_len, up_ptr, up_idx if len(up_idx) else [0], level_ptr, level_reach)]
+    fl = [np.ascontiguousarray(x, np.float32) for x in (qlat_ts_f32, qdp0_f32, dp0_f32, reach_last0_f32)]
+    q, rl = np.zeros(S), np.zeros(R)
+    _check(lib().troute_wavefront_fp64(_ptr(p), *(_ptr(a) for a in ints), R, len(level_ptr) - 1, S,
+                                       *(_ptr(a) for a in fl), _ptr(q), _ptr(rl), int(n_timesteps), float(dt)))
+    return q, rl
+
+
+class Network:
+    """A routed network (or a batch of networks) with device-resident state."""
+
+    def __init__(self, topos, params, dt: float = 300.0, cfg: Cfg | None = None, qlat_col=None, qlat_scale=None,
+                 qlat_cols: int = 0):
+        if isinstance(topos, dict):
+            topos, params = [topos], [params]
+            qlat_col = None if qlat_col is None else [qlat_col]
+            qlat_scale = None if qlat_scale is None else [qlat_scale]
+        n = len(topos)
+        self._keep = []
+        tarr = (Topo * n)()
+        parr = (C.c_void_p * n)()
+        carr = (C.c_void_p * n)()
+        sarr = (C.c_void_p * n)()
+        self.n_segments_each = []
+        self.n_reaches_each = []
+        for i, t in enumerate(topos):
+            ts, keep = _topo_struct(t["reach_seg_start"], t["reach_seg_len"], t["reach_up_ptr"], t["reach_up_idx"],
+                                    t["n_segments"])
+            tarr[i] = ts
+            pp = _params(params[i])
+            self._keep += keep + [pp]
+            parr[i] = pp.ctypes.data
+            self.n_segments_each.append(int(t["n_segments"]))
+            self.n_reaches_each.append(int(len(t["reach_seg_start"])))
+            if qlat_col is not None and qlat_col[i] is not None:
+                c = _i32(qlat_col[i])
+                self._keep.append(c)
+                carr[i] = c.ctypes.data
+            if qlat_scale is not None and qlat_scale[i] is not None:
+                s = _f64(qlat_scale[i])
+                self._keep.append(s)
+                sarr[i] = s.ctypes.data
+        h = C.c_void_p()
+        _check(lib().troute_create_batch(C.byref(h), n, tarr, parr, carr if qlat_col is not None else None,
+                                         sarr if qlat_scale is not None else None, int(qlat_cols), float(dt),
+                                         C.byref(cfg) if cfg is not None else None))
+        self._h = h
+        self._keep = []  # the library copied everything
+        R, S, L, Q, T = _I(), _I(), _I(), _I(), C.c_longlong()
+        _check(lib().troute_info(self._h, C.byref(R), C.byref(S), C.byref(L), C.byref(Q), C.byref(T)))
+        self.n_reaches, self.n_segments, self.n_levels, self.qlat_cols = R.value, S.value, L.value, Q.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().troute_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def steps_done(self) -> int:
+        T = C.c_longlong()
+        _check(lib().troute_info(self._h, None, None, None, None, C.byref(T)))
+        return T.value
+
+    def set_cfg(self, cfg: Cfg):
+        _check(lib().troute_set_cfg(self._h, C.byref(cfg)))
+
+    def set_state(self, qdp, dp, reach_last=None):
+        q = _f64(qdp, self.n_segments)
+        d = _f64(dp, self.n_segments)
+        r = None if reach_last is None else _f64(reach_last, self.n_reaches)
+        _check(lib().troute_set_state(self._h, _ptr(q), _ptr(d), _ptr(r)))
+
+    def get_state(self):
+        q, d, v, r = (np.zeros(self.n_segments), np.zeros(self.n_segments), np.zeros(self.n_segments),
+                      np.zeros(self.n_reaches))
+        _check(lib().troute_get_state(self._h, _ptr(q), _ptr(d), _ptr(v), _ptr(r)))
+        return q, d, v, r
+
+    def run(self, qlat_ts) -> dict:
+        ql = np.ascontiguousarray(qlat_ts, dtype=np.float64)
+        if ql.ndim != 2 or ql.shape[1] != self.qlat_cols:
+            raise ValueError(f"qlat must be [n_ts][{self.qlat_cols}]")
+        st = Stats()
+        _check(lib().troute_run(self._h, _ptr(ql), int(ql.shape[0]), C.byref(st)))
+        return st.as_dict()
+
+    def run_device(self, qlat_dev_ptr: int, n_ts: int, stream: int = 0):
+        _check(lib().troute_run_device(self._h, C.c_void_p(qlat_dev_ptr), int(n_ts), C.c_void_p(stream)))
+
+    def sync(self) -> dict:
+        st = Stats()
+        _check(lib().troute_sync(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def graph_capture(self, qlat_dev_ptr: int, n_ts: int):
+        _check(lib().troute_graph_capture(self._h, C.c_void_p(qlat_dev_ptr), int(n_ts)))
+
+    def graph_launch(self, stream: int = 0):
+        _check(lib().troute_graph_launch(self._h, C.c_void_p(stream)))
+
+    def history(self, n_ts: int):
+        out = np.zeros((n_ts, self.n_segments))
+        _check(lib().troute_get_history(self._h, _ptr(out), int(n_ts)))
+        return out
+
+    def checkpoint(self) -> bytes:
+        n = C.c_size_t(0)
+        _check(lib().troute_checkpoint(self._h, None, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        _check(lib().troute_checkpoint(self._h, buf, C.byref(n)))
+        return buf.raw[: n.value]
+
+    def restore(self, blob: bytes):
+        buf = C.create_string_buffer(blob, len(blob))
+        _check(lib().troute_restore(self._h, buf, len(blob)))
+
+
+def route_tree(topo: dict, params, qlat_ts, qdp0, dp0, reach_last0=None, dt: float = 300.0, cfg: Cfg | None = None,
+               history: bool = False):
+    """One-shot FP64 tree routing; returns dict(q, d, v, reach_last, stats[, q_hist])."""
+    c = cfg if cfg is not None else make_cfg()
+    if history:
+        c = Cfg.from_buffer_copy(c)
+        c.record_history = 1
+    with Network(topo, params, dt=dt, cfg=c) as net:
+        net.set_state(qdp0, dp0, reach_last0)
+        ql = np.ascontiguousarray(qlat_ts, dtype=np.float64)
+        st = net.run(ql)
+        q, d, v, r = net.get_state()
+        out = {"q": q, "d": d, "v": v, "reach_last": r, "stats": st}
+        if history:
+            out["q_hist"] = net.history(ql.shape[0])
+        return out

@@ -1,0 +1,368 @@
+/*
+ * CPU oracle for the t-route Muskingum-Cunge secant routing path.
+ *
+ * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+ * CPU legs of bench.py as the checker. Nothing in the product calls it.
+ *
+ * This is a plain-C restatement of the reference's FP64 CPU routines:
+ *   - oracle_mc_solve  follows cpu_mc's inlined solve,
+ *       water-prediction/t-route/troute_mc_final.cu:181-248
+ *       (device twin mc_solve/hgeo at :30-139);
+ *   - oracle_cpu_mc    follows cpu_mc, troute_mc_final.cu:167-252;
+ *   - oracle_route_tree follows cpu_wavefront_fp64,
+ *       water-prediction/t-route/wavefront/wavefront_mc.cu:495-564,
+ *       with FP64 inputs instead of the reference's float inputs.
+ * The only change of algorithm is that the secant tolerances (rtol/atol,
+ * maxiter, attempts) are parameters; at rtol = atol = 0.01, maxiter = 100,
+ * attempts = 5 the arithmetic is operation-for-operation the reference's
+ * (same association order, no FMA contraction: build with -ffp-contract=off),
+ * which tests/test_oracle_ref.py checks bit-for-bit against the compiled
+ * reference.
+ */
+#include "troute_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MINDEPTH 0.01 /* troute_mc_final.cu:58 */
+
+/* Channel geometry at depth h: trapezoid plus compound (floodplain) channel.
+ * troute_mc_final.cu:30-40 (inlined at :200-205 and :216-221). */
+typedef struct geo {
+    double twl, R, A, AC, WP, WPC;
+} geo;
+
+static void channel_geometry(double h, double bfd, double bw, double twcc, double z,
+                             geo* g)
+{
+    g->twl = bw + 2.0 * z * h;
+    double above = fmax(h - bfd, 0.0);
+    double below = fmin(bfd, h);
+    if (above > 0.0 && twcc <= 0.0) {
+        above = 0.0;
+        below = h;
+    }
+    g->A = (bw + below * z) * below;
+    g->WP = bw + 2.0 * below * sqrt(1.0 + z * z);
+    g->AC = twcc * above;
+    g->WPC = (above > 0.0) ? (twcc + 2.0 * above) : 0.0;
+    g->R = (g->WP + g->WPC > 0.0) ? (g->A + g->AC) / (g->WP + g->WPC) : 0.0;
+}
+
+/* Kinematic celerity from Manning's equation, troute_mc_final.cu:78-82 / :97-101. */
+static double celerity(double h, const geo* g, double s0, double n_ch, double bw, double z)
+{
+    if (!(h > 0.0)) return 0.0;
+    double r23 = pow(g->R, 2.0 / 3.0);
+    double r53 = pow(g->R, 5.0 / 3.0);
+    return fmax(0.0, (sqrt(s0) / n_ch) *
+                         ((5.0 / 3.0) * r23 -
+                          (2.0 / 3.0) * r53 * (2.0 * sqrt(1.0 + z * z) / (bw + 2.0 * h * z))));
+}
+
+/* Manning discharge at the geometry g, troute_mc_final.cu:91 / :111. */
+static double manning_q(const geo* g, double n_ch, double ncc, double s0)
+{
+    if (!(g->WP + g->WPC > 0.0)) return 0.0;
+    return (1.0 / (((g->WP * n_ch) + (g->WPC * ncc)) / (g->WP + g->WPC))) * (g->A + g->AC) *
+           pow(g->R, 2.0 / 3.0) * sqrt(s0);
+}
+
+double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
+                       const oracle_chparams* p, double depthp,
+                       const oracle_tol* tol,
+                       double* depthc, double* velc, int* iters)
+{
+    const double bw = p->bw, tw = p->tw, twcc = p->twcc, n_ch = p->n_ch, ncc = p->ncc;
+    const double s0 = p->s0, dx = p->dx;
+    /* side slope and bankfull depth, :181-183 */
+    const double z = (p->cs == 0.0) ? 1.0 : 1.0 / p->cs;
+    const double bfd = (bw > tw) ? bw / 0.00001 : (bw == tw) ? bw / (2.0 * z) : (tw - bw) / (2.0 * z);
+    *iters = 0;
+
+    /* invalid parameters or no flow at all: zero outputs, :187-190 */
+    if (n_ch <= 0.0 || s0 <= 0.0 || z <= 0.0 || bw <= 0.0 ||
+        (ql <= 0.0 && qup <= 0.0 && quc <= 0.0 && qdp <= 0.0)) {
+        *depthc = 0.0;
+        *velc = 0.0;
+        return 0.0;
+    }
+
+    const double depth = fmax(depthp, 0.0);
+    double h = depth * 1.33 + MINDEPTH; /* upper secant start, :193 */
+    double h_0 = depth * 0.67;          /* lower secant start */
+    double C1 = 0.0, C2 = 0.0, C3 = 0.0, C4 = 0.0, X = 0.25;
+    double Qj_0 = 0.0, Qj;
+    int maxiter = tol->maxiter;
+    int total = 0;
+
+    for (int attempt = 0; attempt < tol->attempts; attempt++) {
+        double aerr = 0.01, rerr = 1.0;
+        int iter = 0;
+        int first = 1; /* the first pass of every attempt always runs */
+        while (first || (rerr > tol->rtol && aerr >= tol->atol && iter <= maxiter)) {
+            first = 0;
+            /* lower point h_0, :200-214 */
+            geo g0;
+            channel_geometry(h_0, bfd, bw, twcc, z, &g0);
+            const double Ck0 = celerity(h_0, &g0, s0, n_ch, bw, z);
+            const double Km0 = (Ck0 > 0.0) ? fmax(dt, dx / Ck0) : dt;
+            const double twu0 = (h_0 > bfd && twcc > 0.0) ? twcc : g0.twl;
+            const double X0 = (Ck0 > 0.0 && twu0 * s0 * Ck0 * dx > 0.0)
+                                  ? fmin(0.5, fmax(0.0, 0.5 * (1.0 - Qj_0 / (2.0 * twu0 * s0 * Ck0 * dx))))
+                                  : 0.5;
+            double D0 = Km0 * (1.0 - X0) + dt / 2.0;
+            if (D0 == 0.0) D0 = 1.0;
+            const double c1 = (Km0 * X0 + dt / 2.0) / D0;
+            const double c2 = (dt / 2.0 - Km0 * X0) / D0;
+            const double c3 = (Km0 * (1.0 - X0) - dt / 2.0) / D0;
+            const double c4 = (ql * dt) / D0;
+            const double qmc0 = c1 * qup + c2 * quc + c3 * qdp + c4;
+            Qj_0 = qmc0 - manning_q(&g0, n_ch, ncc, s0);
+
+            /* upper point h, :216-231; X is clamped to [0.25, 0.5] here and
+             * uses the h_0 coefficients in its numerator */
+            geo g1;
+            channel_geometry(h, bfd, bw, twcc, z, &g1);
+            const double Ck1 = celerity(h, &g1, s0, n_ch, bw, z);
+            const double Km1 = (Ck1 > 0.0) ? fmax(dt, dx / Ck1) : dt;
+            const double twu1 = (h > bfd && twcc > 0.0) ? twcc : g1.twl;
+            X = (Ck1 > 0.0 && twu1 * s0 * Ck1 * dx > 0.0)
+                    ? fmin(0.5, fmax(0.25, 0.5 * (1.0 - qmc0 / (2.0 * twu1 * s0 * Ck1 * dx))))
+                    : 0.5;
+            double D1 = Km1 * (1.0 - X) + dt / 2.0;
+            if (D1 == 0.0) D1 = 1.0;
+            C1 = (Km1 * X + dt / 2.0) / D1;
+            C2 = (dt / 2.0 - Km1 * X) / D1;
+            C3 = (Km1 * (1.0 - X) - dt / 2.0) / D1;
+            C4 = (ql * dt) / D1;
+            if (C4 < 0.0 && fabs(C4) > C1 * qup + C2 * quc + C3 * qdp)
+                C4 = -(C1 * qup + C2 * quc + C3 * qdp);
+            Qj = (C1 * qup + C2 * quc + C3 * qdp + C4) - manning_q(&g1, n_ch, ncc, s0);
+
+            /* secant update, :233-237 */
+            double h_1 = (Qj_0 - Qj != 0.0) ? h - (Qj * (h_0 - h)) / (Qj_0 - Qj) : h;
+            if (h_1 < 0.0) h_1 = h;
+            if (h > 0.0) {
+                rerr = fabs((h_1 - h) / h);
+                aerr = fabs(h_1 - h);
+            } else {
+                rerr = 0.0;
+                aerr = 0.9;
+            }
+            h_0 = fmax(0.0, h);
+            h = fmax(0.0, h_1);
+            iter++;
+            total++;
+            if (h < MINDEPTH) break;
+        }
+        if (iter < maxiter) break;
+        /* widen the bracket and allow more iterations, :240 */
+        h *= 1.33;
+        h_0 *= 0.67;
+        maxiter += 25;
+    }
+
+    /* outflow with the negative-flow fallbacks, :242-244 */
+    double qdc;
+    const double Qmc = C1 * qup + C2 * quc + C3 * qdp + C4;
+    if (Qmc < 0.0) {
+        if (C4 < 0.0 && fabs(C4) > C1 * qup + C2 * quc + C3 * qdp)
+            qdc = 0.0;
+        else
+            qdc = fmax(C1 * qup + C2 * quc + C4, C1 * qup + C3 * qdp + C4);
+    } else {
+        qdc = Qmc;
+    }
+
+    /* velocity from the trapezoid-only hydraulic radius, :245-248 */
+    const double twl = bw + 2.0 * z * h;
+    double Rv = (h * (bw + twl) / 2.0) /
+                (bw + 2.0 * sqrt(((twl - bw) / 2.0) * ((twl - bw) / 2.0) + h * h));
+    if (Rv < 0.0) Rv = 0.0;
+    *velc = (1.0 / n_ch) * pow(Rv, 2.0 / 3.0) * sqrt(s0);
+    *depthc = h;
+    *iters = total;
+    return qdc;
+}
+
+void oracle_cpu_mc(const oracle_chparams* p, const double* ql,
+                   const int* rs, const int* rl,
+                   const double* qu, const double* qd, const double* dp,
+                   double* qo, double* vo, double* dpo,
+                   double uq, double dt, int nr,
+                   const oracle_tol* tol, long long* iters_total)
+{
+    long long total = 0;
+    for (int r = 0; r < nr; r++) {
+        double quc = uq; /* chained current-step inflow, seeded by uq: :175 */
+        for (int i = 0; i < rl[r]; i++) {
+            const int s = rs[r] + i;
+            double dc, vc;
+            int it;
+            const double q = oracle_mc_solve(dt, qu[s], quc, qd[s], ql[s], &p[s], dp[s], tol,
+                                             &dc, &vc, &it);
+            qo[s] = q;
+            vo[s] = vc;
+            dpo[s] = dc;
+            quc = q;
+            total += it;
+        }
+    }
+    if (iters_total) *iters_total = total;
+}
+
+/* ---------------------------------------------------------------------------
+ * Tree routing (wavefront_mc.cu:495-564). State is double-buffered by step
+ * parity instead of the reference's swap + refill; every reach and segment is
+ * rewritten each step, so the values are the same.
+ * ------------------------------------------------------------------------- */
+typedef struct tree_job {
+    const int *seg_start, *seg_len, *up_ptr, *up_idx, *level_ptr, *level_reach;
+    int n_reaches, n_levels, n_segments;
+    const oracle_chparams* params;
+    const double* qlat_ts;
+    int n_ts;
+    double dt;
+    const oracle_tol* tol;
+    double *q[2], *d[2], *v, *rl[2];
+    double* q_hist;
+    int n_threads;
+    pthread_barrier_t barrier;
+} tree_job;
+
+typedef struct tree_worker {
+    tree_job* job;
+    int rank;
+    long long iters;
+} tree_worker;
+
+static void route_reach(tree_job* J, int r, int t, long long* iters)
+{
+    const int prev = t & 1, cur = (t + 1) & 1;
+    const double* qlat = J->qlat_ts + (size_t)t * (size_t)J->n_segments;
+    /* upstream sums at the reach head, :525-531 */
+    double qup_head = 0.0, quc_head = 0.0;
+    for (int k = J->up_ptr[r]; k < J->up_ptr[r + 1]; ++k) {
+        const int u = J->up_idx[k];
+        qup_head += J->rl[prev][u];
+        quc_head += J->rl[cur][u];
+    }
+    double quc_next = 0.0, q_last = 0.0;
+    const int s0 = J->seg_start[r];
+    for (int i = 0; i < J->seg_len[r]; ++i) {
+        const int s = s0 + i;
+        /* interior segments take the upstream segment's previous and current
+         * discharge, :538-539 */
+        const double qup = (i == 0) ? qup_head : J->q[prev][s - 1];
+        const double quc = (i == 0) ? quc_head : quc_next;
+        double dc, vc;
+        int it;
+        const double q = oracle_mc_solve(J->dt, qup, quc, J->q[prev][s], qlat[s], &J->params[s],
+                                         J->d[prev][s], J->tol, &dc, &vc, &it);
+        J->q[cur][s] = q;
+        J->d[cur][s] = dc;
+        J->v[s] = vc;
+        if (J->q_hist) J->q_hist[(size_t)t * (size_t)J->n_segments + s] = q;
+        quc_next = q;
+        q_last = q;
+        *iters += it;
+    }
+    J->rl[cur][r] = q_last;
+}
+
+static void* tree_worker_main(void* arg)
+{
+    tree_worker* W = (tree_worker*)arg;
+    tree_job* J = W->job;
+    for (int t = 0; t < J->n_ts; ++t) {
+        for (int L = 0; L < J->n_levels; ++L) {
+            const int lb = J->level_ptr[L], le = J->level_ptr[L + 1];
+            const int n = le - lb;
+            const int per = (n + J->n_threads - 1) / J->n_threads;
+            const int b = lb + W->rank * per;
+            const int e = (b + per < le) ? b + per : le;
+            for (int ii = b; ii < e; ++ii) route_reach(J, J->level_reach[ii], t, &W->iters);
+            if (J->n_threads > 1) pthread_barrier_wait(&J->barrier);
+        }
+    }
+    return NULL;
+}
+
+int oracle_route_tree(const int* reach_seg_start, const int* reach_seg_len,
+                      const int* reach_up_ptr, const int* reach_up_idx,
+                      const int* level_ptr, const int* level_reach,
+                      int n_reaches, int n_levels, int n_segments,
+                      const oracle_chparams* params, const double* qlat_ts,
+                      const double* qdp0, const double* dp0, const double* reach_last0,
+                      int n_ts, double dt, const oracle_tol* tol,
+                      double* q_out, double* d_out, double* v_out,
+                      double* reach_last_out, double* q_hist,
+                      long long* iters_total, int n_threads)
+{
+    if (n_reaches < 0 || n_segments < 0 || n_levels < 0 || n_ts < 0) return 1;
+    if (n_threads < 1) n_threads = 1;
+    tree_job J;
+    memset(&J, 0, sizeof J);
+    J.seg_start = reach_seg_start;
+    J.seg_len = reach_seg_len;
+    J.up_ptr = reach_up_ptr;
+    J.up_idx = reach_up_idx;
+    J.level_ptr = level_ptr;
+    J.level_reach = level_reach;
+    J.n_reaches = n_reaches;
+    J.n_levels = n_levels;
+    J.n_segments = n_segments;
+    J.params = params;
+    J.qlat_ts = qlat_ts;
+    J.n_ts = n_ts;
+    J.dt = dt;
+    J.tol = tol;
+    J.q_hist = q_hist;
+    J.n_threads = n_threads;
+    const size_t S = (size_t)n_segments, R = (size_t)n_reaches;
+    double* buf = (double*)calloc(4 * S + 2 * R + 1, sizeof(double));
+    if (!buf) return 2;
+    J.q[0] = buf;
+    J.q[1] = buf + S;
+    J.d[0] = buf + 2 * S;
+    J.d[1] = buf + 3 * S;
+    J.rl[0] = buf + 4 * S;
+    J.rl[1] = buf + 4 * S + R;
+    J.v = v_out;
+    memcpy(J.q[0], qdp0, S * sizeof(double));
+    memcpy(J.d[0], dp0, S * sizeof(double));
+    memcpy(J.rl[0], reach_last0, R * sizeof(double));
+    memset(v_out, 0, S * sizeof(double));
+
+    long long total = 0;
+    if (n_threads == 1) {
+        tree_worker W = {&J, 0, 0};
+        tree_worker_main(&W);
+        total = W.iters;
+    } else {
+        pthread_barrier_init(&J.barrier, NULL, (unsigned)n_threads);
+        tree_worker* W = (tree_worker*)calloc((size_t)n_threads, sizeof(tree_worker));
+        pthread_t* th = (pthread_t*)calloc((size_t)n_threads, sizeof(pthread_t));
+        for (int i = 0; i < n_threads; ++i) {
+            W[i].job = &J;
+            W[i].rank = i;
+            if (i > 0) pthread_create(&th[i], NULL, tree_worker_main, &W[i]);
+        }
+        tree_worker_main(&W[0]);
+        for (int i = 1; i < n_threads; ++i) pthread_join(th[i], NULL);
+        for (int i = 0; i < n_threads; ++i) total += W[i].iters;
+        pthread_barrier_destroy(&J.barrier);
+        free(W);
+        free(th);
+    }
+    const int fin = n_ts & 1;
+    memcpy(q_out, J.q[fin], S * sizeof(double));
+    memcpy(d_out, J.d[fin], S * sizeof(double));
+    memcpy(reach_last_out, J.rl[fin], R * sizeof(double));
+    if (iters_total) *iters_total = total;
+    free(buf);
+    return 0;
+}

@@ -1,0 +1,77 @@
+/*
+ * CPU oracle for the t-route Muskingum-Cunge secant routing path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the checker that the CUDA path is
+ * compared against; it is called only by tests/, by __graft_entry__.smoke() and
+ * by bench.py's CPU-baseline / reference legs. The product (libtroute_gb300.so
+ * and the troute_gb300 Python package) never links, loads or calls it.
+ *
+ * Pinned against the reference itself: tests/test_oracle_ref.py compiles the
+ * reference's own cpu_mc (water-prediction/t-route/troute_mc_final.cu:167-252)
+ * and cpu_wavefront_fp64 (water-prediction/t-route/wavefront/wavefront_mc.cu:
+ * 495-564) and checks this restatement bit-for-bit at the reference tolerance;
+ * tests/golden/ holds fixtures produced by those compiled reference routines.
+ */
+#ifndef TROUTE_ORACLE_H
+#define TROUTE_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Per-segment channel parameters, same member order and size as the
+ * reference's ChParams (troute_mc_final.cu:26-28). */
+typedef struct oracle_chparams {
+    double dx, bw, tw, twcc, n_ch, ncc, cs, s0;
+} oracle_chparams;
+
+/* Secant tolerances. The reference hardcodes rtol = atol = 0.01, maxiter = 100,
+ * 5 attempts (troute_mc_final.cu:69-74). */
+typedef struct oracle_tol {
+    double rtol;
+    double atol;
+    int maxiter;
+    int attempts;
+} oracle_tol;
+
+/* One segment solve (troute_mc_final.cu:42-139 / :181-248). Returns qdc and
+ * writes depth, velocity and the number of secant iterations run. */
+double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
+                       const oracle_chparams* p, double depthp,
+                       const oracle_tol* tol,
+                       double* depthc, double* velc, int* iters);
+
+/* Reach-parallel single step, the reference's cpu_mc (troute_mc_final.cu:167-252)
+ * with tolerances as a parameter. iters_total may be NULL. */
+void oracle_cpu_mc(const oracle_chparams* p, const double* ql,
+                   const int* rs, const int* rl,
+                   const double* qu, const double* qd, const double* dp,
+                   double* qo, double* vo, double* dpo,
+                   double uq, double dt, int nr,
+                   const oracle_tol* tol, long long* iters_total);
+
+/* Level-scheduled multi-step tree routing in FP64, the semantics of the
+ * reference's cpu_wavefront_fp64 (wavefront_mc.cu:495-564) with FP64
+ * parameters and lateral inflow.
+ *   qlat_ts   [n_ts][n_segments]
+ *   q_hist    optional [n_ts][n_segments] per-step discharge (may be NULL)
+ *   q_out/d_out/v_out  final-step discharge/depth/velocity per segment
+ *   reach_last_out     final-step discharge of each reach's last segment
+ * n_threads <= 1 runs single-threaded; otherwise the reaches of each level are
+ * split over n_threads POSIX threads with a barrier between levels (results are
+ * identical: reaches within a level are independent). */
+int oracle_route_tree(const int* reach_seg_start, const int* reach_seg_len,
+                      const int* reach_up_ptr, const int* reach_up_idx,
+                      const int* level_ptr, const int* level_reach,
+                      int n_reaches, int n_levels, int n_segments,
+                      const oracle_chparams* params, const double* qlat_ts,
+                      const double* qdp0, const double* dp0, const double* reach_last0,
+                      int n_ts, double dt, const oracle_tol* tol,
+                      double* q_out, double* d_out, double* v_out,
+                      double* reach_last_out, double* q_hist,
+                      long long* iters_total, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

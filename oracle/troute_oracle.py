@@ -1,0 +1,217 @@
+"""ctypes access to the CPU oracle and, where it was built, to the compiled
+reference routines.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU legs of bench.py as the checker. The product package never imports it.
+
+  oracle_cpu_mc / oracle_route_tree   our C restatement (troute_oracle.c),
+      built into oracle/_build/libtroute_oracle.so by `make -C oracle oracle`;
+  ref_cpu_mc / ref_cpu_wavefront_fp64  the reference's own cpu_mc
+      (water-prediction/t-route/troute_mc_final.cu:167-252) and
+      cpu_wavefront_fp64 (water-prediction/t-route/wavefront/wavefront_mc.cu:
+      495-564), compiled unmodified into oracle/_ref/libtroute_ref.so by
+      `make -C oracle ref` where the reference checkout exists.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libtroute_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libtroute_ref.so")
+REF_ROOT = os.environ.get("TROUTE_REF_ROOT", "/root/reference")
+
+CHP = np.dtype([(n, "<f8") for n in ("dx", "bw", "tw", "twcc", "n_ch", "ncc", "cs", "s0")])
+CHP32 = np.dtype([(n, "<f4") for n in ("dx", "bw", "tw", "twcc", "n_ch", "ncc", "cs", "s0")])
+
+
+class Tol(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("maxiter", C.c_int), ("attempts", C.c_int)]
+
+
+REF_TOL = (0.01, 0.01, 100, 5)
+
+
+def build(ref: bool = True) -> None:
+    """Builds the oracle (always) and the reference library (when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    if ref and os.path.exists(os.path.join(REF_ROOT, "water-prediction", "t-route", "troute_mc_final.cu")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={REF_ROOT}"], check=True)
+
+
+_ORC = None
+_REF = None
+_P = C.c_void_p
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def oracle():
+    global _ORC
+    if _ORC is None:
+        if not os.path.exists(ORACLE_SO):
+            build(ref=False)
+        L = C.CDLL(ORACLE_SO)
+        L.oracle_cpu_mc.argtypes = [_P] * 10 + [C.c_double, C.c_double, C.c_int, _P, _P]
+        L.oracle_cpu_mc.restype = None
+        L.oracle_route_tree.argtypes = [_P] * 6 + [C.c_int] * 3 + [_P] * 5 + [C.c_int, C.c_double, _P] + [_P] * 6 + [C.c_int]
+        L.oracle_route_tree.restype = C.c_int
+        L.oracle_mc_solve.argtypes = [C.c_double] * 5 + [_P, C.c_double, _P, _P, _P, _P]
+        L.oracle_mc_solve.restype = C.c_double
+        _ORC = L
+    return _ORC
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref():
+    global _REF
+    if _REF is None:
+        L = C.CDLL(REF_SO)
+        L.ref_cpu_mc.argtypes = [_P] * 10 + [C.c_double, C.c_double, C.c_int]
+        L.ref_cpu_mc.restype = None
+        L.ref_cpu_wavefront_fp64.argtypes = [_P] * 7 + [C.c_int] * 3 + [_P] * 6 + [C.c_int, C.c_double]
+        L.ref_cpu_wavefront_fp64.restype = None
+        _REF = L
+    return _REF
+
+
+def _tol(t):
+    return Tol(*t) if not isinstance(t, Tol) else t
+
+
+def _params(p):
+    p = np.ascontiguousarray(p)
+    if p.dtype.names is not None:
+        return np.ascontiguousarray(p.astype(CHP))
+    return np.ascontiguousarray(np.asarray(p, np.float64).reshape(-1, 8)).view(CHP).reshape(-1)
+
+
+def cpu_mc(p, ql, rs, rl, qu, qd, dp, uq=10.0, dt=300.0, tol=REF_TOL):
+    """Oracle restatement of cpu_mc -> (qo, vo, dpo, iterations)."""
+    p = _params(p)
+    n = p.shape[0]
+    ql, qu, qd, dp = (np.ascontiguousarray(x, np.float64) for x in (ql, qu, qd, dp))
+    rs, rl = np.ascontiguousarray(rs, np.int32), np.ascontiguousarray(rl, np.int32)
+    qo, vo, dpo = np.zeros(n), np.zeros(n), np.zeros(n)
+    it = C.c_longlong()
+    t = _tol(tol)
+    oracle().oracle_cpu_mc(_ptr(p), _ptr(ql), _ptr(rs), _ptr(rl), _ptr(qu), _ptr(qd), _ptr(dp), _ptr(qo), _ptr(vo),
+                           _ptr(dpo), float(uq), float(dt), int(rs.size), C.byref(t), C.byref(it))
+    return qo, vo, dpo, it.value
+
+
+def mc_solve(dt, qup, quc, qdp, ql, p_record, depthp, tol=REF_TOL):
+    """One segment solve -> (q, depth, velocity, iterations)."""
+    p = _params(np.asarray(p_record).reshape(1, -1) if np.asarray(p_record).dtype.names is None else p_record)
+    d, v, it = C.c_double(), C.c_double(), C.c_int()
+    t = _tol(tol)
+    q = oracle().oracle_mc_solve(dt, qup, quc, qdp, ql, _ptr(p), depthp, C.byref(t), C.byref(d), C.byref(v),
+                                 C.byref(it))
+    return q, d.value, v.value, it.value
+
+
+def route_tree(topo, params, qlat_ts, qdp0, dp0, reach_last0, dt=300.0, tol=REF_TOL, history=False, threads=1,
+               level_ptr=None, level_reach=None):
+    """Oracle tree routing (cpu_wavefront_fp64 semantics, FP64 inputs)."""
+    seg_start = np.ascontiguousarray(topo["reach_seg_start"], np.int32)
+    seg_len = np.ascontiguousarray(topo["reach_seg_len"], np.int32)
+    up_ptr = np.ascontiguousarray(topo["reach_up_ptr"], np.int32)
+    up_idx = np.ascontiguousarray(topo["reach_up_idx"] if len(topo["reach_up_idx"]) else [0], np.int32)
+    R, S = seg_start.size, int(topo["n_segments"])
+    if level_ptr is None:
+        level_ptr, level_reach = levels(up_ptr, up_idx, R)
+    level_ptr = np.ascontiguousarray(level_ptr, np.int32)
+    level_reach = np.ascontiguousarray(level_reach, np.int32)
+    p = _params(params)
+    ql = np.ascontiguousarray(qlat_ts, np.float64)
+    T = ql.shape[0]
+    q0, d0, r0 = (np.ascontiguousarray(x, np.float64) for x in (qdp0, dp0, reach_last0))
+    q, d, v, rl = np.zeros(S), np.zeros(S), np.zeros(S), np.zeros(R)
+    hist = np.zeros((T, S)) if history else None
+    it = C.c_longlong()
+    t = _tol(tol)
+    rc = oracle().oracle_route_tree(_ptr(seg_start), _ptr(seg_len), _ptr(up_ptr), _ptr(up_idx), _ptr(level_ptr),
+                                    _ptr(level_reach), R, level_ptr.size - 1, S, _ptr(p), _ptr(ql), _ptr(q0), _ptr(d0),
+                                    _ptr(r0), T, float(dt), C.byref(t), _ptr(q), _ptr(d), _ptr(v), _ptr(rl),
+                                    _ptr(hist), C.byref(it), int(threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_route_tree failed: {rc}")
+    out = {"q": q, "d": d, "v": v, "reach_last": rl, "iterations": it.value}
+    if history:
+        out["q_hist"] = hist
+    return out
+
+
+def levels(up_ptr, up_idx, R):
+    """Reference level construction (gen_network.py:219-231), numpy only."""
+    up_ptr = np.asarray(up_ptr)
+    up_idx = np.asarray(up_idx)
+    down = np.full(R, -1)
+    for r in range(R):
+        for k in range(up_ptr[r], up_ptr[r + 1]):
+            down[up_idx[k]] = r
+    indeg = np.diff(up_ptr).copy()
+    order = [r for r in range(R) if indeg[r] == 0]
+    i = 0
+    while i < len(order):
+        d = down[order[i]]
+        if d >= 0:
+            indeg[d] -= 1
+            if indeg[d] == 0:
+                order.append(d)
+        i += 1
+    level = np.zeros(R, np.int32)
+    for r in order:
+        ups = up_idx[up_ptr[r]:up_ptr[r + 1]]
+        if len(ups):
+            level[r] = 1 + level[ups].max()
+    L = int(level.max()) + 1 if R else 0
+    level_reach = np.argsort(level, kind="stable").astype(np.int32)
+    counts = np.bincount(level, minlength=L).astype(np.int32)
+    level_ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    return level_ptr, level_reach
+
+
+def ref_cpu_mc(p, ql, rs, rl, qu, qd, dp, uq=10.0, dt=300.0):
+    """The reference's own cpu_mc (compiled from its source)."""
+    p = _params(p)
+    n = p.shape[0]
+    ql, qu, qd, dp = (np.ascontiguousarray(x, np.float64) for x in (ql, qu, qd, dp))
+    rs, rl = np.ascontiguousarray(rs, np.int32), np.ascontiguousarray(rl, np.int32)
+    qo, vo, dpo = np.zeros(n), np.zeros(n), np.zeros(n)
+    ref().ref_cpu_mc(_ptr(p), _ptr(ql), _ptr(rs), _ptr(rl), _ptr(qu), _ptr(qd), _ptr(dp), _ptr(qo), _ptr(vo),
+                     _ptr(dpo), float(uq), float(dt), int(rs.size))
+    return qo, vo, dpo
+
+
+def ref_wavefront_fp64(topo, params_f32, qlat_f32, qdp0_f32, dp0_f32, reach_last0_f32, dt=300.0,
+                       level_ptr=None, level_reach=None):
+    """The reference's own cpu_wavefront_fp64 -> (q_final, reach_last_final)."""
+    seg_start = np.ascontiguousarray(topo["reach_seg_start"], np.int32)
+    seg_len = np.ascontiguousarray(topo["reach_seg_len"], np.int32)
+    up_ptr = np.ascontiguousarray(topo["reach_up_ptr"], np.int32)
+    up_idx = np.ascontiguousarray(topo["reach_up_idx"] if len(topo["reach_up_idx"]) else [0], np.int32)
+    R, S = seg_start.size, int(topo["n_segments"])
+    if level_ptr is None:
+        level_ptr, level_reach = levels(up_ptr, up_idx, R)
+    level_ptr = np.ascontiguousarray(level_ptr, np.int32)
+    level_reach = np.ascontiguousarray(level_reach, np.int32)
+    p = np.ascontiguousarray(params_f32)
+    if p.dtype != CHP32:
+        p = np.ascontiguousarray(np.asarray(p, np.float32).reshape(-1, 8)).view(CHP32).reshape(-1)
+    ql = np.ascontiguousarray(qlat_f32, np.float32)
+    q0, d0, r0 = (np.ascontiguousarray(x, np.float32) for x in (qdp0_f32, dp0_f32, reach_last0_f32))
+    q, rl = np.zeros(S), np.zeros(R)
+    ref().ref_cpu_wavefront_fp64(_ptr(p), _ptr(seg_start), _ptr(seg_len), _ptr(up_ptr), _ptr(up_idx),
+                                 _ptr(level_ptr), _ptr(level_reach), R, level_ptr.size - 1, S, _ptr(ql), _ptr(q0),
+                                 _ptr(d0), _ptr(r0), _ptr(q), _ptr(rl), int(ql.shape[0]), float(dt))
+    return q, rl

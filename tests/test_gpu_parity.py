@@ -1,0 +1,256 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the
+reference-made golden fixtures.
+
+Bars (relative error on discharge, and on depth / velocity where stated):
+  - reference tolerance (rtol = atol = 0.01): whole multi-step trajectories,
+    every step, 1e-10;
+  - rtol = 1e-8: one step at a time from a state both sides share, 1e-10.
+    (Multi-step trajectories at 1e-8 are not comparable below ~1e-4 by any
+    implementation that is not bit-identical to the host libm: the oracle
+    itself moves that much under a 1-ulp input change, see
+    test_oracle.py::test_tight_tolerance_trajectories_are_ulp_sensitive.)
+"""
+import os
+
+import numpy as np
+import pytest
+
+import troute_gb300 as T
+from golden_inputs import GOLDEN, make_golden
+from oracle import troute_oracle as O
+from troute_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+TIGHT = (1e-8, 1e-10, 100, 5)
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    den = np.maximum(np.abs(b), 1e-300)
+    e = np.where((a == b), 0.0, np.abs(a - b) / den)
+    return float(e.max()) if e.size else 0.0
+
+
+def cfg_of(tol, **kw):
+    return T.make_cfg(rtol=tol[0], atol=tol[1], maxiter=tol[2], attempts=tol[3], **kw)
+
+
+# ---------------------------------------------------------------- reach-parallel
+def test_reach_parallel_matches_reference_golden():
+    p, ql, rs, rl, qu, qd, dp = make_golden.cpu_mc_inputs()
+    g = np.load(os.path.join(GOLDEN, "cpu_mc_c0.npz"))
+    qo, vo, dpo, st = T.mc_reach_parallel(p, ql, rs, rl, qu, qd, dp, uq=10.0, dt=300.0, return_stats=True)
+    assert rel_err(qo, g["qo"]) < REL
+    assert rel_err(dpo, g["dpo"]) < REL
+    assert rel_err(vo, g["vo"]) < REL
+    assert st["solves"] == len(qo) and st["early_exits"] >= 6
+
+
+def test_reach_parallel_tight_tolerance_matches_oracle():
+    p, ql, rs, rl, qu, qd, dp = make_golden.cpu_mc_inputs()
+    a = O.cpu_mc(p, ql, rs, rl, qu, qd, dp, tol=TIGHT)
+    qo, vo, dpo, st = T.mc_reach_parallel(p, ql, rs, rl, qu, qd, dp, cfg=cfg_of(TIGHT), return_stats=True)
+    assert rel_err(qo, a[0]) < REL and rel_err(dpo, a[2]) < REL and rel_err(vo, a[1]) < REL
+    assert st["iterations"] == a[3]
+
+
+# ---------------------------------------------------------------- tree, reference tolerance
+@pytest.mark.parametrize("T_", [1, 24, 288])
+def test_wavefront_fp64_dropin_matches_reference_golden(T_):
+    topo, p32, ql32, q0, d0, r0 = make_golden.wavefront_inputs()
+    g = np.load(os.path.join(GOLDEN, "wavefront_c0.npz"))
+    lp, lr = O.levels(topo["reach_up_ptr"], topo["reach_up_idx"], len(topo["reach_seg_start"]))
+    q, rl = T.wavefront_fp64(p32, topo["reach_seg_start"], topo["reach_seg_len"], topo["reach_up_ptr"],
+                             topo["reach_up_idx"], lp, lr, ql32[:T_], q0, d0, r0, T_, 300.0)
+    assert rel_err(q, g[f"q_{T_}"]) < REL
+    assert rel_err(rl, g[f"reach_last_{T_}"]) < REL
+
+
+def test_tree_full_history_matches_oracle_reference_tol():
+    c = synth.network("c0")
+    args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    o = O.route_tree(*args, history=True)
+    g = T.route_tree(*args, history=True)
+    for t in range(c["n_ts"]):
+        assert rel_err(g["q_hist"][t], o["q_hist"][t]) < REL, t
+    assert rel_err(g["d"], o["d"]) < REL and rel_err(g["v"], o["v"]) < REL
+    assert rel_err(g["reach_last"], o["reach_last"]) < REL
+    assert g["stats"]["iterations"] == o["iterations"]
+
+
+# ---------------------------------------------------------------- tree, tight tolerance
+def _oracle_state(c, t, tol):
+    """Oracle state after t steps: (q, d, reach_last)."""
+    if t == 0:
+        return c["q0"], c["d0"], c["rl0"]
+    o = O.route_tree(c["topo"], c["params"], c["qlat"][:t], c["q0"], c["d0"], c["rl0"], tol=tol)
+    return o["q"], o["d"], o["reach_last"]
+
+
+@pytest.mark.parametrize("t", [0, 5, 60, 287])
+def test_tree_one_step_tight_tolerance_matches_oracle(t):
+    c = synth.network("c0")
+    q, d, rl = _oracle_state(c, t, TIGHT)
+    o = O.route_tree(c["topo"], c["params"], c["qlat"][t:t + 1], q, d, rl, tol=TIGHT)
+    g = T.route_tree(c["topo"], c["params"], c["qlat"][t:t + 1], q, d, rl, cfg=cfg_of(TIGHT))
+    assert rel_err(g["q"], o["q"]) < REL
+    assert rel_err(g["d"], o["d"]) < REL
+    assert rel_err(g["v"], o["v"]) < REL
+
+
+def test_tree_tight_tolerance_trajectory_statistics():
+    """Whole 288-step run at 1e-8: iteration counts agree within 1% and the
+    network outflow agrees closely (the trajectories are ulp-sensitive)."""
+    c = synth.network("c0")
+    args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    o = O.route_tree(*args, tol=TIGHT)
+    g = T.route_tree(*args, cfg=cfg_of(TIGHT))
+    assert abs(g["stats"]["iterations"] - o["iterations"]) <= 0.01 * o["iterations"]
+    assert abs(g["q"].sum() - o["q"].sum()) <= 1e-3 * o["q"].sum()
+
+
+# ---------------------------------------------------------------- structure and edge cases
+def _topo(seg_len, ups):
+    seg_len = np.asarray(seg_len, np.int32)
+    return {"n_segments": int(seg_len.sum()),
+            "reach_seg_start": np.concatenate([[0], np.cumsum(seg_len)[:-1]]).astype(np.int32),
+            "reach_seg_len": seg_len,
+            "reach_up_ptr": np.concatenate([[0], np.cumsum([len(u) for u in ups])]).astype(np.int32),
+            "reach_up_idx": np.array([x for u in ups for x in u], np.int32)}
+
+
+@pytest.mark.parametrize("case", ["y", "zero_len", "single", "isolated", "wide", "invalid", "dry"])
+def test_edge_cases_match_oracle(case):
+    rng = np.random.default_rng(3)
+    if case == "y":
+        topo = _topo([3, 2, 4], [[], [], [0, 1]])
+    elif case == "zero_len":
+        topo = _topo([2, 0, 3, 1], [[], [], [0, 1], [2]])
+    elif case == "single":
+        topo = _topo([1], [[]])
+    elif case == "isolated":
+        topo = _topo([1] * 70, [[]] * 70)
+    elif case == "wide":   # one reach with 40 upstream reaches (max fan-in case)
+        topo = _topo([1] * 40 + [5], [[]] * 40 + [list(range(40))])
+    else:
+        topo = _topo([3, 3, 2], [[], [], [0, 1]])
+    S = topo["n_segments"]
+    params = synth.make_params(77, S)
+    qlat = synth.make_qlat(77, S, 12)
+    q0 = np.full(S, 0.1)
+    d0 = np.full(S, 0.1)
+    rl0 = np.full(len(topo["reach_seg_start"]), 0.1)
+    if case == "invalid":
+        params["n_ch"][1] = 0.0
+        params["bw"][4] = -1.0
+    if case == "dry":
+        qlat[:] = 0.0
+        q0[:] = 0.0
+        rl0[:] = 0.0
+    o = O.route_tree(topo, params, qlat, q0, d0, rl0, history=True)
+    g = T.route_tree(topo, params, qlat, q0, d0, rl0, history=True)
+    assert rel_err(g["q_hist"], o["q_hist"]) < REL
+    assert rel_err(g["d"], o["d"]) < REL and rel_err(g["reach_last"], o["reach_last"]) < REL
+    if case == "dry":
+        assert not g["q"].any()
+
+
+def test_zero_steps_and_empty_network():
+    c = synth.network("c0", n_ts=1)
+    g = T.route_tree(c["topo"], c["params"], c["qlat"][:0], c["q0"], c["d0"], c["rl0"])
+    np.testing.assert_array_equal(g["q"], c["q0"])
+    with T.Network(_topo([], []), np.zeros((0, 8))) as net:
+        assert net.n_reaches == 0
+        net.run(np.zeros((3, 0)))
+
+
+def test_batch_equals_separate_runs():
+    nets = [synth.network(f"tree:{S}", seed=s, n_ts=20) for S, s in ((1500, 1), (400, 2), (3000, 3))]
+    cols = sum(n["topo"]["n_segments"] for n in nets)
+    qlat = np.concatenate([n["qlat"] for n in nets], axis=1)
+    with T.Network([n["topo"] for n in nets], [n["params"] for n in nets]) as b:
+        assert b.qlat_cols == cols
+        b.set_state(np.concatenate([n["q0"] for n in nets]), np.concatenate([n["d0"] for n in nets]),
+                    np.concatenate([n["rl0"] for n in nets]))
+        b.run(qlat)
+        qb, db, vb, rb = b.get_state()
+    off = 0
+    for n in nets:
+        S = n["topo"]["n_segments"]
+        s = T.route_tree(n["topo"], n["params"], n["qlat"], n["q0"], n["d0"], n["rl0"])
+        np.testing.assert_array_equal(qb[off:off + S], s["q"])
+        np.testing.assert_array_equal(db[off:off + S], s["d"])
+        off += S
+
+
+def test_ensemble_column_map_and_scale():
+    c = synth.network("tree:2000", seed=4, n_ts=10)
+    S = c["topo"]["n_segments"]
+    qf, nf = synth.make_member(5, 1, S)
+    p1 = c["params"].copy()
+    p1["n_ch"] *= nf
+    p1["ncc"] *= nf
+    with T.Network([c["topo"], c["topo"]], [c["params"], p1], qlat_col=[np.arange(S), np.arange(S)],
+                   qlat_scale=[None, qf], qlat_cols=S) as b:
+        b.set_state(np.tile(c["q0"], 2), np.tile(c["d0"], 2), np.tile(c["rl0"], 2))
+        b.run(c["qlat"])
+        qb = b.get_state()[0]
+    o0 = O.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    o1 = O.route_tree(c["topo"], p1, c["qlat"] * qf[None, :], c["q0"], c["d0"], c["rl0"])
+    assert rel_err(qb[:S], o0["q"]) < REL and rel_err(qb[S:], o1["q"]) < REL
+
+
+def test_checkpoint_resume_is_bit_identical():
+    c = synth.network("c0", n_ts=40)
+    with T.Network(c["topo"], c["params"]) as a:
+        a.set_state(c["q0"], c["d0"], c["rl0"])
+        a.run(c["qlat"][:15])
+        blob = a.checkpoint()
+        a.run(c["qlat"][15:])
+        full = a.get_state()
+    with T.Network(c["topo"], c["params"]) as b:
+        b.restore(blob)
+        assert b.steps_done == 15
+        b.run(c["qlat"][15:])
+        resumed = b.get_state()
+    for x, y in zip(full, resumed):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_launch_shape_does_not_change_results():
+    c = synth.network("tree:20000", seed=8, n_ts=16)
+    outs = []
+    for tpb, bps in ((128, 0), (64, 1), (32, 2)):
+        cfg = T.make_cfg(threads_per_block=tpb, blocks_per_sm=bps)
+        outs.append(T.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"], cfg=cfg)["q"])
+    for x in outs[1:]:
+        np.testing.assert_array_equal(x, outs[0])
+
+
+def test_bounded_wait_times_out_cleanly():
+    assert T.timeout_probe(200_000) == 5   # TROUTE_ETIMEOUT
+    c = synth.network("c0", n_ts=3)        # context still usable
+    g = T.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    o = O.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    assert rel_err(g["q"], o["q"]) < REL
+
+
+def test_tiny_wait_budget_reports_timeout_or_completes():
+    """With a wait budget of a few cycles the run either finishes (no wait was
+    needed) or returns TROUTE_ETIMEOUT; it never hangs, and the handle
+    refuses further runs until its state is reset."""
+    c = synth.network("tree:50000", seed=9, n_ts=8)
+    with T.Network(c["topo"], c["params"], cfg=T.make_cfg(wait_cycles=1)) as net:
+        net.set_state(c["q0"], c["d0"], c["rl0"])
+        try:
+            net.run(c["qlat"])
+        except T.TrouteError as e:
+            assert e.code == 5
+            with pytest.raises(T.TrouteError) as e2:
+                net.run(c["qlat"])
+            assert e2.value.code == 8
+            net.set_state(c["q0"], c["d0"], c["rl0"])
+            net.set_cfg(T.make_cfg())
+            net.run(c["qlat"])

@@ -1,0 +1,148 @@
+"""The CPU oracle against the reference: golden fixtures made by the
+reference's own compiled routines, and (where the reference checkout exists)
+the compiled reference itself on fresh inputs."""
+import os
+
+import numpy as np
+import pytest
+
+from golden_inputs import GOLDEN, make_golden
+from oracle import troute_oracle as O
+
+
+def test_cpu_mc_matches_golden():
+    p, ql, rs, rl, qu, qd, dp = make_golden.cpu_mc_inputs()
+    g = np.load(os.path.join(GOLDEN, "cpu_mc_c0.npz"))
+    assert make_golden.sha(p, ql, rs, rl, qu, qd, dp) == str(g["input_sha"])
+    qo, vo, dpo, _ = O.cpu_mc(p, ql, rs, rl, qu, qd, dp, uq=10.0, dt=300.0)
+    np.testing.assert_array_equal(qo, g["qo"])
+    np.testing.assert_array_equal(vo, g["vo"])
+    np.testing.assert_array_equal(dpo, g["dpo"])
+    # edge cases really were exercised: invalid parameters give zeros
+    for s in (5, 17, 23):
+        assert qo[s] == 0.0 and vo[s] == 0.0 and dpo[s] == 0.0
+
+
+@pytest.mark.parametrize("T", [1, 24, 288])
+def test_wavefront_matches_golden(T):
+    topo, p32, ql32, q0, d0, r0 = make_golden.wavefront_inputs()
+    g = np.load(os.path.join(GOLDEN, "wavefront_c0.npz"))
+    assert make_golden.sha(topo["reach_seg_start"], topo["reach_seg_len"], topo["reach_up_ptr"],
+                           topo["reach_up_idx"], p32, ql32, q0, d0, r0) == str(g["input_sha"])
+    o = O.route_tree(topo, p32.astype(np.float64), ql32[:T].astype(np.float64), q0.astype(np.float64),
+                     d0.astype(np.float64), r0.astype(np.float64))
+    np.testing.assert_array_equal(o["q"], g[f"q_{T}"])
+    np.testing.assert_array_equal(o["reach_last"], g[f"reach_last_{T}"])
+
+
+def _reference_gen(seed, nr):
+    """Inputs shaped like the reference's own gen() (troute_mc_final.cu:254-274)."""
+    rng = np.random.default_rng(seed)
+    rl = rng.integers(1, 21, nr).astype(np.int32)
+    rs = np.concatenate([[0], np.cumsum(rl)[:-1]]).astype(np.int32)
+    S = int(rl.sum())
+    p = np.zeros((S, 8))
+    p[:, 0] = 500.0 + rng.integers(0, 5000, S)
+    p[:, 1] = 5.0 + rng.integers(0, 50, S)
+    p[:, 2] = p[:, 1] + rng.integers(0, 20, S)
+    p[:, 3] = p[:, 2] + rng.integers(0, 100, S)
+    p[:, 4] = 0.02 + 0.06 * rng.random(S)
+    p[:, 5] = p[:, 4] * 1.5
+    p[:, 6] = 0.5 + 2.0 * rng.random(S)
+    p[:, 7] = 0.0001 + 0.005 * rng.random(S)
+    ql = 0.5 * rng.random(S)
+    bq = 5.0 + 50.0 * rng.random(S)
+    return p, ql, rs, rl, bq * 0.95, bq, 0.5 + 3.0 * rng.random(S)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference checkout not present")
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_cpu_mc_matches_compiled_reference(seed):
+    p, ql, rs, rl, qu, qd, dp = _reference_gen(seed, 400)
+    a = O.cpu_mc(p, ql, rs, rl, qu, qd, dp, uq=10.0, dt=300.0)
+    b = O.ref_cpu_mc(p, ql, rs, rl, qu, qd, dp, uq=10.0, dt=300.0)
+    for x, y in zip(a[:3], b):
+        np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference checkout not present")
+def test_wavefront_matches_compiled_reference_other_seed():
+    from troute_gb300 import synth
+
+    c = synth.network("tree:3000", seed=99, n_ts=12)
+    p32 = np.asarray(c["params"].view("<f8").reshape(-1, 8), np.float32)
+    ql32 = c["qlat"].astype(np.float32)
+    q0 = np.random.default_rng(5).uniform(0.0, 15.0, c["topo"]["n_segments"]).astype(np.float32)
+    d0 = np.random.default_rng(6).uniform(0.3, 3.0, c["topo"]["n_segments"]).astype(np.float32)
+    r0 = np.random.default_rng(7).uniform(0.0, 10.0, len(c["topo"]["reach_seg_start"])).astype(np.float32)
+    qr, rlr = O.ref_wavefront_fp64(c["topo"], p32, ql32, q0, d0, r0)
+    o = O.route_tree(c["topo"], p32.astype(np.float64), ql32.astype(np.float64), q0.astype(np.float64),
+                     d0.astype(np.float64), r0.astype(np.float64))
+    np.testing.assert_array_equal(o["q"], qr)
+    np.testing.assert_array_equal(o["reach_last"], rlr)
+
+
+def test_threaded_oracle_identical():
+    from troute_gb300 import synth
+
+    c = synth.network("c0", n_ts=48)
+    a = O.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"], threads=1)
+    b = O.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"], threads=3)
+    for k in ("q", "d", "v", "reach_last"):
+        np.testing.assert_array_equal(a[k], b[k])
+    assert a["iterations"] == b["iterations"]
+
+
+def test_tolerance_parameter():
+    """At the reference tolerance the parameterised loop is the reference's;
+    a tighter tolerance runs more iterations, and one step from a common state
+    at 1e-8 and at 1e-10 agrees to well below 1e-6."""
+    from troute_gb300 import synth
+
+    c = synth.network("c0", n_ts=24)
+    args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    a = O.route_tree(*args, tol=(0.01, 0.01, 100, 5))
+    b = O.route_tree(*args, tol=(1e-8, 1e-10, 100, 5))
+    assert b["iterations"] > a["iterations"]
+    # single segment solves (no chaining): the iteration's limit is reached
+    p = c["params"]
+    rel = []
+    for s in range(0, 1000, 7):
+        a8 = O.mc_solve(300.0, 0.3, 0.35, 0.1, c["qlat"][0, s], p[s:s + 1], 0.1, tol=(1e-8, 1e-10, 100, 5))
+        a10 = O.mc_solve(300.0, 0.3, 0.35, 0.1, c["qlat"][0, s], p[s:s + 1], 0.1, tol=(1e-10, 1e-12, 100, 5))
+        assert a10[3] >= a8[3]
+        if a10[3] <= 100:   # a tighter run that exhausts maxiter restarts from a wider bracket
+            rel.append(abs(a8[0] - a10[0]) / abs(a10[0]))
+    assert len(rel) > 100 and max(rel) < 1e-6
+
+
+def test_tight_tolerance_trajectories_are_ulp_sensitive():
+    """Property of the reference algorithm that sets how multi-step parity is
+    tested: its two secant residuals use different X clamps (troute_mc_final.cu
+    :86 vs :105), so the iteration converges linearly to a point that depends
+    on the starting bracket, i.e. on the previous depth. At rtol = 1e-8 a 1-ulp
+    change of one step's lateral inflow grows to >1e-4 over the run; at the
+    reference tolerance it stays below 1e-10."""
+    from troute_gb300 import synth
+
+    c = synth.network("c0", n_ts=96)
+    ql2 = c["qlat"].copy()
+    ql2[0] = np.nextafter(ql2[0], np.inf)
+    for tol, lo, hi in (((1e-8, 1e-10, 100, 5), 1e-4, 1.0), ((0.01, 0.01, 100, 5), 0.0, 1e-10)):
+        a = O.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"], tol=tol)
+        b = O.route_tree(c["topo"], c["params"], ql2, c["q0"], c["d0"], c["rl0"], tol=tol)
+        rel = (np.abs(a["q"] - b["q"]) / np.maximum(np.abs(a["q"]), 1e-300)).max()
+        assert lo <= rel < hi, (tol, rel)
+
+
+def test_planted_mistake_is_caught():
+    """A deliberately wrong oracle run (lateral inflow scaled by 1 + 1e-9)
+    must fail the 1e-10 discharge parity bar used by the GPU tests."""
+    from troute_gb300 import synth
+
+    c = synth.network("c0", n_ts=24)
+    a = O.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"], tol=(1e-8, 1e-10, 100, 5))
+    b = O.route_tree(c["topo"], c["params"], c["qlat"] * (1 + 1e-9), c["q0"], c["d0"], c["rl0"],
+                     tol=(1e-8, 1e-10, 100, 5))
+    rel = np.abs(a["q"] - b["q"]) / np.maximum(np.abs(a["q"]), 1e-300)
+    assert rel.max() > 1e-10
