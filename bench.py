@@ -250,7 +250,7 @@ def run_ours(args, dist: Dist):
     qlat_host = torch.empty((n_ts, S), dtype=torch.float64, pin_memory=True)
     qlat_host.numpy()[:] = w["qlat"]
     qlat_dev = qlat_host.to(dev, non_blocking=False)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)   # a real stream: 0 would mean "the handle's own stream"
     net.graph_capture(qlat_dev.data_ptr(), n_ts)
     for _ in range(args.warmup):
         net.graph_launch(stream.cuda_stream)

@@ -60,7 +60,10 @@ typedef struct troute_cfg {
     int warm_start;         /* 1: learned warm start (needs troute_set_warm_start) */
     int warm_k;             /* iterations a warm-started solve gets before the plain solve */
     int record_history;     /* 1: keep per-step discharge of every segment (troute_get_history) */
-    int reserved[7];
+    int mapping;            /* reach-to-warp mapping: 0 auto (3), 1 one level-block per
+                               warp, 2 per-lane refill in level-block order,
+                               3 per-lane refill from the ready queue */
+    int reserved[6];
 } troute_cfg;
 
 /* Counters of one run (summed over all segment solves). */
@@ -72,6 +75,10 @@ typedef struct troute_stats {
     unsigned long long warm_used;     /* solves that started from the learned depth */
     unsigned long long warm_fallback; /* warm-started solves that fell back to the plain secant */
     unsigned long long iter_hist[16]; /* iterations per solve, last bin = 15+ */
+    unsigned long long warp_passes;   /* passes of the per-lane refill loop (mapping 2) */
+    unsigned long long lane_busy;     /* lane-passes spent evaluating a depth */
+    unsigned long long lane_wait;     /* lane-passes waiting for inputs */
+    unsigned long long lane_idle;     /* lane-passes with no work */
     double kernel_ms;                 /* device time of the routing kernel(s) */
     int timeout;                      /* 1 if a bounded wait ran out */
     int reserved[3];
@@ -194,6 +201,11 @@ int troute_restore(troute_handle* h, const void* buf, size_t nbytes);
  * wait_cycles; returns TROUTE_ETIMEOUT once the wait gives up and the context
  * stays usable. Exercises the device failure path without faulting. */
 int troute_debug_timeout_probe(long long wait_cycles);
+
+/* Evaluates, on the device, the solver's pow(x, 2/3) and pow(x, 5/3) for n
+ * host values: out = [ours_23[n], ours_53[n], cuda_pow_23[n], cuda_pow_53[n]]
+ * (the last two from CUDA's pow(), for accuracy checks). */
+int troute_debug_pow(const double* x, int n, double* out);
 
 /* ---- schedule and topology helpers ----------------------------------- */
 /* Topological levels as the reference builds them (level 0 = headwater,

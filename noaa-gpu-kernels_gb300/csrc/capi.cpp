@@ -182,6 +182,22 @@ extern "C" int troute_debug_timeout_probe(long long wait_cycles)
     return set_error(TROUTE_ESTATE, "probe did not report a timeout");
 }
 
+extern "C" int troute_debug_pow(const double* x, int n, double* out)
+{
+    if (n < 0 || (n > 0 && (!x || !out))) return set_error(TROUTE_EINVAL, "bad arguments");
+    if (n == 0) return TROUTE_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(TROUTE_ENODEV, "no CUDA device");
+    DevPtr dx, dout;
+    int rc;
+    if ((rc = cuda_check(cudaMalloc(&dx.p, (size_t)n * sizeof(double)), "cudaMalloc")) ||
+        (rc = cuda_check(cudaMalloc(&dout.p, (size_t)4 * n * sizeof(double)), "cudaMalloc")) ||
+        (rc = cuda_check(cudaMemcpy(dx.p, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice), "H2D")))
+        return rc;
+    if ((rc = launch_debug_pow(static_cast<double*>(dx.p), n, static_cast<double*>(dout.p), nullptr))) return rc;
+    return cuda_check(cudaMemcpy(out, dout.p, (size_t)4 * n * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+}
+
 // ---------------------------------------------------------------------------
 // topology helpers
 // ---------------------------------------------------------------------------

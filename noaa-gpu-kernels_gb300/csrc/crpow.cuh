@@ -1,0 +1,167 @@
+// Correctly rounded pow(x, 2.0/3.0) and pow(x, 5.0/3.0) in double precision,
+// host and device. (The exponents are the doubles nearest 2/3 and 5/3, as in
+// the reference's pow calls; steps 1-3 work with the rationals and step 4
+// applies the exponent offset.)
+//
+// The MC solver raises the hydraulic radius R to the powers 2/3 and 5/3 at
+// every depth it evaluates (troute_mc_final.cu:80, :91, :99, :111, :136); this
+// is where most of its FP64 work went with the general pow(). Both powers come
+// from one inverse cube root:
+//   1. write x = y * 2^(3k) with y in [1, 8) (exact exponent split);
+//   2. seed r ~ y^(-1/3) in single precision (hardware log2/exp2 on the GPU,
+//      ~2^-22 relative), then one Newton step for f(r) = y r^3 - 1 in double
+//      precision, r <- r + r (1 - y r^3) / 3 (quadratic: ~2^-43);
+//   3. z = y r ~ y^(2/3) to ~2^-42; the residual d = z^3 - y^2 is evaluated
+//      exactly enough with error-free products (a*b = p + fma(a, b, -p), the
+//      FMA form of Dekker's TwoProduct), and one more Newton step gives the
+//      correction delta = -d / (3 z^2) = -d r^4 / 3 (z is within a factor 2 of
+//      the root, so q - s below is exact), leaving z + delta within ~2^-84 of
+//      y^(2/3);
+//   4. the exponent offset e = fl(2/3) - 2/3 contributes the factor
+//      1 + e ln x (|e ln x| < 1e-13), so pow(x, fl(2/3)) =
+//      round(z + (delta + z e ln x)) and pow(x, fl(5/3)) =
+//      round(y z + (err(y z) + y delta + y z e' ln x)), each scaled back by
+//      2^(2k), 2^(5k) (exact).
+// The rounding of step 4 is therefore the correctly rounded result except when
+// the exact value lies within ~2^-84 relative of a rounding midpoint. The
+// host C library's pow() is correctly rounded in all but rare cases, so the
+// device solver reproduces the host computation bit for bit almost always.
+// Only IEEE operations and explicit fma() are used, so compiling without
+// implicit FMA contraction does not change these results.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#if defined(__CUDACC__)
+#define CRPOW_HD __host__ __device__ __forceinline__
+#else
+#define CRPOW_HD inline
+#include <cmath>
+#endif
+
+namespace tr {
+
+CRPOW_HD uint64_t crpow_bits(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+
+CRPOW_HD double crpow_from_bits(uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    std::memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+
+// Single-precision log2(y) and seed of y^(-1/3) for y in [1, 8).
+CRPOW_HD void crpow_seed(double y, double* log2y, double* rinv)
+{
+#if defined(__CUDA_ARCH__)
+    const float yf = (float)y;
+    float l, r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l) : "f"(yf));
+    const float e = l * (-1.0f / 3.0f);
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(e));
+    *log2y = (double)l;
+    *rinv = (double)r;
+#else
+    *log2y = (double)std::log2((float)y);
+    *rinv = (double)(1.0f / std::cbrt((float)y));
+#endif
+}
+
+// 2^n as a double for |n| <= 1022 (exact)
+CRPOW_HD double crpow_exp2i(int n) { return crpow_from_bits((uint64_t)(1023 + n) << 52); }
+
+// Scales v by 2^n (n may exceed the single-step range); exact for normal results.
+CRPOW_HD double crpow_scale(double v, int n)
+{
+    while (n > 1000) { v *= crpow_exp2i(1000); n -= 1000; }
+    while (n < -1000) { v *= crpow_exp2i(-1000); n += 1000; }
+    return v * crpow_exp2i(n);
+}
+
+// fl(2/3) - 2/3 = -(1/3) 2^-53 and fl(5/3) - 5/3 = (1/3) 2^-52
+constexpr double kFl23Minus23 = -3.700743415417188e-17;
+constexpr double kFl53Minus53 = 7.401486830834377e-17;
+
+// x^fl(2/3) and x^fl(5/3), both correctly rounded (see above). x < 0 gives NaN,
+// x = 0 gives 0, +inf gives +inf, NaN propagates, like pow().
+CRPOW_HD void pow23_53(double x, double* p23, double* p53)
+{
+    if (!(x > 0.0)) {
+        const double v = (x == 0.0) ? 0.0 : (x - x) / (x - x);  // 0 or NaN
+        *p23 = v;
+        *p53 = v;
+        return;
+    }
+    uint64_t b = crpow_bits(x);
+    int ex = (int)((b >> 52) & 0x7FF);
+    if (ex == 0x7FF) {  // inf (NaN fails x > 0 above)
+        *p23 = x;
+        *p53 = x;
+        return;
+    }
+    int shift = 0;
+    if (ex == 0) {  // subnormal: lift into the normal range first
+        x *= crpow_exp2i(54);
+        b = crpow_bits(x);
+        ex = (int)((b >> 52) & 0x7FF);
+        shift = 54;
+    }
+    const int e = ex - 1023 - shift;                   // x = m 2^e, m in [1, 2)
+    const int k = (e >= 0) ? e / 3 : -((-e + 2) / 3);  // floor(e / 3)
+    const int j = e - 3 * k;                           // 0, 1, 2
+    const double y = crpow_from_bits((b & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(1023 + j) << 52));
+
+    const double third = 1.0 / 3.0;
+    double r, log2y;
+    crpow_seed(y, &log2y, &r);
+    {
+        const double r3 = (r * r) * r;
+        const double g = fma(-y, r3, 1.0);  // 1 - y r^3
+        r = fma(r * g, third, r);
+    }
+    const double z = y * r;  // ~ y^(2/3)
+    // d = z^3 - y^2 with error-free products
+    const double p = z * z;
+    const double pe = fma(z, z, -p);
+    const double q = z * p;
+    const double qe = fma(z, p, -q);
+    const double t = z * pe;
+    const double s = y * y;
+    const double se = fma(y, y, -s);
+    const double d = (q - s) + ((qe + t) - se);
+    const double r2 = r * r;
+    const double delta = -(d * (r2 * r2)) * third;
+    // exponent offset: x^fl(2/3) = x^(2/3) (1 + (fl(2/3) - 2/3) ln x), same for 5/3;
+    // ln x needs only ~1e-3 relative accuracy here (the term is ~1e-16 x^(2/3))
+    const double lnx = (log2y + 3.0 * (double)k) * 0.6931471805599453;
+    const double c2 = kFl23Minus23 * lnx, c5 = kFl53Minus53 * lnx;
+    const double z23 = z + (delta + z * c2);
+    const double w0 = y * z;
+    const double we = fma(y, z, -w0);
+    const double z53 = w0 + ((we + y * delta) + w0 * c5);
+    *p23 = crpow_scale(z23, 2 * k);
+    *p53 = crpow_scale(z53, 5 * k);
+}
+
+CRPOW_HD double pow23(double x)
+{
+    double a, b;
+    pow23_53(x, &a, &b);
+    return a;
+}
+
+}  // namespace tr

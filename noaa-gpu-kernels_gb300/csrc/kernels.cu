@@ -23,68 +23,9 @@
 // TROUTE_ETIMEOUT and every warp returns.
 #include <cuda_runtime.h>
 
-#include "mc_solve.cuh"
+#include "device_common.cuh"
 
 namespace tr {
-
-__device__ __forceinline__ int ld_acquire(const int* p)
-{
-    int v;
-    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release(int* p, int v)
-{
-    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ int ld_volatile_int(const int* p)
-{
-    return *reinterpret_cast<const volatile int*>(p);
-}
-
-__device__ void record_error(DevStats* st, int code, int reach, int step, int where)
-{
-    if (atomicCAS(&st->error, 0, code) == 0) {
-        st->err_reach = reach;
-        st->err_step = step;
-        st->err_where = where;
-    }
-}
-
-// Per-thread counters, folded into the block's shared copy at the end.
-struct LocalStats {
-    unsigned long long solves, iterations, retries, early;
-};
-
-__device__ __forceinline__ void count_solve(LocalStats& ls, unsigned int* hist_s, const SolveOut& o)
-{
-    ls.solves++;
-    ls.iterations += (unsigned)o.iters;
-    ls.retries += (unsigned)o.retried;
-    ls.early += (unsigned)o.early;
-    atomicAdd(&hist_s[o.iters < 15 ? o.iters : 15], 1u);
-}
-
-__device__ void flush_stats(LocalStats& ls, unsigned int* hist_s, DevStats* st)
-{
-    // warp reduce, one atomic per warp
-    for (int off = 16; off > 0; off >>= 1) {
-        ls.solves += __shfl_down_sync(0xffffffffu, ls.solves, off);
-        ls.iterations += __shfl_down_sync(0xffffffffu, ls.iterations, off);
-        ls.retries += __shfl_down_sync(0xffffffffu, ls.retries, off);
-        ls.early += __shfl_down_sync(0xffffffffu, ls.early, off);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&st->solves, ls.solves);
-        atomicAdd(&st->iterations, ls.iterations);
-        atomicAdd(&st->retries, ls.retries);
-        atomicAdd(&st->early_exits, ls.early);
-    }
-    __syncthreads();
-    if (threadIdx.x < 16 && hist_s[threadIdx.x]) atomicAdd(&st->hist[threadIdx.x], (unsigned long long)hist_s[threadIdx.x]);
-}
 
 // ---------------------------------------------------------------------------
 // Reach-parallel single step: the drop-in for kernel_mc_gpu / cpu_mc
@@ -128,34 +69,6 @@ __global__ void __launch_bounds__(256) reach_parallel_kernel(
 // ---------------------------------------------------------------------------
 // Persistent time-skewed tree routing.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int find_wave(const unsigned long long* __restrict__ wave_ptr,
-                                         int n_waves, unsigned long long k)
-{
-    // largest w with wave_ptr[w] <= k
-    int lo = 0, hi = n_waves - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(wave_ptr + mid) <= k) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-// Waits until *flag >= want; false on timeout or when another warp failed.
-__device__ __forceinline__ bool wait_at_least(const int* flag, int want, long long budget,
-                                              DevStats* st)
-{
-    if (ld_acquire(flag) >= want) return true;
-    const long long t0 = clock64();
-    unsigned ns = 32;
-    while (true) {
-        __nanosleep(ns);
-        if (ld_acquire(flag) >= want) return true;
-        if (ns < 1024) ns <<= 1;
-        if (clock64() - t0 > budget) return false;
-        if (ld_volatile_int(&st->error) != 0) return false;
-    }
-}
-
 __global__ void __launch_bounds__(128) route_kernel(NetDev net, RunDev run)
 {
     __shared__ unsigned int hist_s[16];
@@ -293,6 +206,40 @@ __global__ void timeout_probe_kernel(DevStats* st, long long wait_cycles)
     }
 }
 
+// Velocity of every segment from its final depth, the reference's formula
+// (troute_mc_final.cu:132-136; zero for the invalid-parameter exit, :54-56).
+// The per-lane kernels store discharge and depth only; velocity feeds no later
+// solve, so it is derived once per run here.
+__global__ void velocity_kernel(NetDev net)
+{
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < net.n_seg_int;
+         s += (long long)gridDim.x * blockDim.x) {
+        const SegP p = load_seg(net, s);
+        double vel = 0.0;
+        if (!(p.n_ch <= 0.0 || p.s0 <= 0.0 || p.z <= 0.0 || p.bw <= 0.0)) {
+            const double h = __ldcg(net.d + s);
+            const double twl = p.bw + 2.0 * p.z * h;
+            double Rv = (h * (p.bw + twl) / 2.0) /
+                        (p.bw + 2.0 * sqrt(((twl - p.bw) / 2.0) * ((twl - p.bw) / 2.0) + h * h));
+            if (Rv < 0.0) Rv = 0.0;
+            vel = p.inv_n * pow23(Rv) * p.sq_s0;
+        }
+        __stcg(net.v + s, vel);
+    }
+}
+
+__global__ void debug_pow_kernel(const double* __restrict__ x, int n, double* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double a, b;
+        pow23_53(x[i], &a, &b);
+        out[i] = a;
+        out[n + i] = b;
+        out[2 * n + i] = pow(x[i], 2.0 / 3.0);
+        out[3 * n + i] = pow(x[i], 5.0 / 3.0);
+    }
+}
+
 static int cuda_status(cudaError_t e, const char* what)
 {
     if (e == cudaSuccess) return TROUTE_OK;
@@ -358,6 +305,20 @@ int launch_gather(const double* src, const long long* map, long long n, double* 
     if (n <= 0) return TROUTE_OK;
     gather_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(src, map, n, dst);
     return cuda_status(cudaGetLastError(), "gather launch");
+}
+
+int launch_velocity(const NetDev& net, void* stream)
+{
+    if (net.n_seg_int <= 0) return TROUTE_OK;
+    velocity_kernel<<<grid_for(net.n_seg_int, 256), 256, 0, (cudaStream_t)stream>>>(net);
+    return cuda_status(cudaGetLastError(), "velocity launch");
+}
+
+int launch_debug_pow(const double* x, int n, double* out, void* stream)
+{
+    if (n <= 0) return TROUTE_OK;
+    debug_pow_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(x, n, out);
+    return cuda_status(cudaGetLastError(), "debug pow launch");
 }
 
 int launch_timeout_probe(DevStats* stats, long long wait_cycles, void* stream)

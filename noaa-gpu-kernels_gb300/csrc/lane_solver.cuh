@@ -1,0 +1,218 @@
+// Per-lane secant solver shared by the persistent routing kernels that give
+// every lane its own (reach, step): the lane state, the start of a segment
+// solve and one "pass" (one depth evaluation plus its secant bookkeeping).
+//
+// A pass does, for every lane in SOLVE or VEL mode, exactly one evaluation of
+// R^fl(2/3) and R^fl(5/3) (pow23_53), so the expensive part of the pass runs
+// for all busy lanes of a warp together.
+// The evaluation is at h_0 when a solve starts or restarts (need0), otherwise
+// at h followed by the secant update and the stop test.
+// When a solve stops, the segment's discharge and depth are stored and the next
+// segment starts in the same pass; after the reach's last segment the lane goes
+// to DONE and the kernel publishes the reach. The velocity, an output that no
+// later solve reads, is computed once per run from the final depth
+// (velocity_kernel), with the reference's formula (troute_mc_final.cu:132-136).
+// The arithmetic is mc_solve's (mc_solve.cuh, the reference's
+// troute_mc_final.cu:42-139) split at its evaluations, operation for
+// operation.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace tr {
+
+enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_DONE = 4 };
+
+// Everything a lane carries for one (reach, step) and the segment it solves.
+struct Lane {
+    int mode;
+    int ri, tau, g, ns, i, ub, ue, dn;
+    long long base;        // tile slot of segment 0
+    long long wait_t0;
+    double qup_head, quc_head, q_up_old, q_up_new, q_last;
+    // current segment
+    long long s;
+    SegP p;
+    double qup, quc, qdp, ql;
+    double h, h_0, Qj_0, qdc;
+    DepthEval e0;
+    int need0, iter, attempt, maxiter, total, retried;
+};
+
+// Starts segment L.i of the lane's reach; consecutive segments that exit early
+// (invalid parameters or no flow at all, troute_mc_final.cu:54-63) are stored
+// right away. Returns true when a secant solve is pending, false when the reach
+// is complete.
+__device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const RunDev& run,
+                                              LocalStats& ls, unsigned int* hist_s)
+{
+    const double* qlat_row = run.qlat + (size_t)L.tau * (size_t)run.qlat_ld;
+    while (L.i < L.ns) {
+        L.s = L.base + (long long)L.i * kLanes;
+        L.qdp = __ldcg(net.q + L.s);
+        const double dpp = __ldcg(net.d + L.s);
+        L.ql = __ldg(qlat_row + __ldg(net.qcol + L.s));
+        if (net.qscale) L.ql *= __ldg(net.qscale + L.s);
+        L.p = load_seg(net, L.s);
+        L.qup = (L.i == 0) ? L.qup_head : L.q_up_old;
+        L.quc = (L.i == 0) ? L.quc_head : L.q_up_new;
+        const SegP& p = L.p;
+        if (p.n_ch <= 0.0 || p.s0 <= 0.0 || p.z <= 0.0 || p.bw <= 0.0 ||
+            (L.ql <= 0.0 && L.qup <= 0.0 && L.quc <= 0.0 && L.qdp <= 0.0)) {
+            __stcg(net.q + L.s, 0.0);
+            __stcg(net.d + L.s, 0.0);
+            __stcg(net.v + L.s, 0.0);
+            if (run.q_hist) __stcg(run.q_hist + (size_t)L.tau * (size_t)net.n_seg_int + L.s, 0.0);
+            L.q_up_old = L.qdp;
+            L.q_up_new = 0.0;
+            L.q_last = 0.0;
+            SolveOut o;
+            o.iters = 0;
+            o.retried = 0;
+            o.early = 1;
+            count_solve(ls, hist_s, o);
+            ++L.i;
+            continue;
+        }
+        const double depth = fmax(dpp, 0.0);
+        L.h = depth * 1.33 + kMinDepth;
+        L.h_0 = depth * 0.67;
+        L.Qj_0 = 0.0;
+        L.qdc = 0.0;
+        L.maxiter = run.tol.maxiter;
+        L.attempt = 0;
+        L.iter = 0;
+        L.total = 0;
+        L.retried = 0;
+        L.need0 = 1;
+        return true;
+    }
+    return false;
+}
+
+// One evaluation pass of a lane in SOLVE or VEL mode (no-op otherwise).
+__device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunDev& run, LocalStats& ls,
+                                          unsigned int* hist_s)
+{
+    const Tol& tol = run.tol;
+    const double dt = run.dt;
+    if (L.mode == L_SOLVE) {
+        const SegP& p = L.p;
+        const double x = L.need0 ? L.h_0 : L.h;
+        const double twl = p.bw + 2.0 * p.z * x;
+        double above = fmax(x - p.bfd, 0.0);
+        double below = fmin(p.bfd, x);
+        if (above > 0.0 && p.twcc <= 0.0) {
+            above = 0.0;
+            below = x;
+        }
+        const double A = (p.bw + below * p.z) * below;
+        const double WP = p.bw + 2.0 * below * p.sq_1z2;
+        const double AC = p.twcc * above;
+        const double WPC = (above > 0.0) ? (p.twcc + 2.0 * above) : 0.0;
+        const double P = WP + WPC;
+        const double R = (P > 0.0) ? (A + AC) / P : 0.0;
+        double r23, r53;
+        pow23_53(R, &r23, &r53);
+        {
+            DepthEval e;
+            e.Ck = 0.0;
+            if (x > 0.0)
+                e.Ck = fmax(0.0, p.ck_fac * ((5.0 / 3.0) * r23 -
+                                             (2.0 / 3.0) * r53 * (2.0 * p.sq_1z2 / (p.bw + 2.0 * x * p.z))));
+            e.Km = (e.Ck > 0.0) ? fmax(dt, p.dx / e.Ck) : dt;
+            e.twu = (x > p.bfd && p.twcc > 0.0) ? p.twcc : twl;
+            e.Qmn = (P > 0.0) ? (1.0 / ((WP * p.n_ch + WPC * p.ncc) / P)) * (A + AC) * r23 * p.sq_s0 : 0.0;
+            if (L.need0) {
+                L.e0 = e;
+                L.need0 = 0;
+            } else {
+                const double qup = L.qup, quc = L.quc, qdp = L.qdp, ql = L.ql;
+                const DepthEval& e0 = L.e0;
+                const double X0 = (e0.Ck > 0.0 && e0.twu * p.s0 * e0.Ck * p.dx > 0.0)
+                                      ? fmin(0.5, fmax(0.0, 0.5 * (1.0 - L.Qj_0 / (2.0 * e0.twu * p.s0 * e0.Ck * p.dx))))
+                                      : 0.5;
+                double D0 = e0.Km * (1.0 - X0) + dt / 2.0;
+                if (D0 == 0.0) D0 = 1.0;
+                const double c1 = (e0.Km * X0 + dt / 2.0) / D0;
+                const double c2 = (dt / 2.0 - e0.Km * X0) / D0;
+                const double c3 = (e0.Km * (1.0 - X0) - dt / 2.0) / D0;
+                const double c4 = (ql * dt) / D0;
+                const double qmc0 = c1 * qup + c2 * quc + c3 * qdp + c4;
+                L.Qj_0 = qmc0 - e0.Qmn;
+                const double X = (e.Ck > 0.0 && e.twu * p.s0 * e.Ck * p.dx > 0.0)
+                                     ? fmin(0.5, fmax(0.25, 0.5 * (1.0 - qmc0 / (2.0 * e.twu * p.s0 * e.Ck * p.dx))))
+                                     : 0.5;
+                double D1 = e.Km * (1.0 - X) + dt / 2.0;
+                if (D1 == 0.0) D1 = 1.0;
+                const double C1 = (e.Km * X + dt / 2.0) / D1;
+                const double C2 = (dt / 2.0 - e.Km * X) / D1;
+                const double C3 = (e.Km * (1.0 - X) - dt / 2.0) / D1;
+                double C4 = (ql * dt) / D1;
+                if (C4 < 0.0 && fabs(C4) > C1 * qup + C2 * quc + C3 * qdp) C4 = -(C1 * qup + C2 * quc + C3 * qdp);
+                const double Qj = (C1 * qup + C2 * quc + C3 * qdp + C4) - e.Qmn;
+                // outflow of the last evaluated coefficients (troute_mc_final.cu:125-130)
+                const double Qmc = C1 * qup + C2 * quc + C3 * qdp + C4;
+                if (Qmc < 0.0) {
+                    if (C4 < 0.0 && fabs(C4) > C1 * qup + C2 * quc + C3 * qdp)
+                        L.qdc = 0.0;
+                    else
+                        L.qdc = fmax(C1 * qup + C2 * quc + C4, C1 * qup + C3 * qdp + C4);
+                } else {
+                    L.qdc = Qmc;
+                }
+                const double h = L.h;
+                double h_1 = (L.Qj_0 - Qj != 0.0) ? h - (Qj * (L.h_0 - h)) / (L.Qj_0 - Qj) : h;
+                if (h_1 < 0.0) h_1 = h;
+                double rerr, aerr;
+                if (h > 0.0) {
+                    rerr = fabs((h_1 - h) / h);
+                    aerr = fabs(h_1 - h);
+                } else {
+                    rerr = 0.0;
+                    aerr = 0.9;
+                }
+                L.h_0 = fmax(0.0, h);
+                L.h = fmax(0.0, h_1);
+                L.e0 = e;
+                ++L.iter;
+                ++L.total;
+                const bool stop = (L.h < kMinDepth) || !(rerr > tol.rtol && aerr >= tol.atol && L.iter <= L.maxiter);
+                if (stop) {
+                    bool done = true;
+                    if (L.iter >= L.maxiter) {
+                        // widen the bracket (also after the last attempt, as the reference does)
+                        L.h *= 1.33;
+                        L.h_0 *= 0.67;
+                        L.maxiter += 25;
+                        L.retried = 1;
+                        if (++L.attempt < tol.attempts) {
+                            L.iter = 0;
+                            L.need0 = 1;
+                            done = false;
+                        }
+                    }
+                    if (done) {
+                        // store the segment (its velocity is derived from the final depth
+                        // once the run is over, see velocity_kernel) and start the next one
+                        __stcg(net.q + L.s, L.qdc);
+                        __stcg(net.d + L.s, L.h);
+                        if (run.q_hist) __stcg(run.q_hist + (size_t)L.tau * (size_t)net.n_seg_int + L.s, L.qdc);
+                        L.q_up_old = L.qdp;
+                        L.q_up_new = L.qdc;
+                        L.q_last = L.qdc;
+                        SolveOut o;
+                        o.iters = L.total;
+                        o.retried = L.retried;
+                        o.early = 0;
+                        count_solve(ls, hist_s, o);
+                        ++L.i;
+                        L.mode = begin_segment(L, net, run, ls, hist_s) ? L_SOLVE : L_DONE;
+                    }
+                }
+            }
+        }
+    }
+}
+
+}  // namespace tr

@@ -11,6 +11,10 @@
 //   - up to `attempts` bracket-widening restarts (:121-122);
 //   - outflow with the negative-flow fallbacks and trapezoid-only velocity
 //     (:125-138).
+// R^(2/3) and R^(5/3) come from pow23_53 (crpow.cuh), correctly rounded like
+// the host pow() of the reference almost always is; with FMA contraction
+// disabled for this code (the library builds it with -fmad=false) every other
+// operation rounds exactly as the reference's C does.
 // One change of evaluation, not of values: every quantity that depends only on
 // the lower depth h_0 (geometry, Ck, K, Manning discharge) is carried over from
 // the previous iteration's upper-depth evaluation, because each iteration sets
@@ -18,6 +22,7 @@
 // function of the same number. Only a restart (h_0 *= 0.67) re-evaluates it.
 #pragma once
 
+#include "crpow.cuh"
 #include "troute_internal.h"
 
 namespace tr {
@@ -37,8 +42,6 @@ struct DepthEval {
     double Ck, Km, twu, Qmn;
 };
 
-__device__ __forceinline__ double pow23(double x) { return pow(x, 2.0 / 3.0); }
-__device__ __forceinline__ double pow53(double x) { return pow(x, 5.0 / 3.0); }
 
 __device__ __forceinline__ DepthEval eval_depth(double h, const SegP& p, double dt)
 {
@@ -55,11 +58,11 @@ __device__ __forceinline__ DepthEval eval_depth(double h, const SegP& p, double 
     const double WPC = (above > 0.0) ? (p.twcc + 2.0 * above) : 0.0;
     const double P = WP + WPC;
     const double R = (P > 0.0) ? (A + AC) / P : 0.0;
-    const double r23 = pow23(R);
+    double r23, r53;
+    pow23_53(R, &r23, &r53);
     DepthEval e;
     e.Ck = 0.0;
     if (h > 0.0) {
-        const double r53 = pow53(R);
         e.Ck = fmax(0.0, p.ck_fac * ((5.0 / 3.0) * r23 -
                                      (2.0 / 3.0) * r53 * (2.0 * p.sq_1z2 / (p.bw + 2.0 * h * p.z))));
     }

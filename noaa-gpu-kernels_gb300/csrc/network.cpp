@@ -65,6 +65,7 @@ int check_cfg(const troute_cfg& c)
     if (c.threads_per_block != 0 && (c.threads_per_block % 32 != 0 || c.threads_per_block > 128))
         return set_error(TROUTE_EINVAL, "cfg.threads_per_block must be a multiple of 32, at most 128");
     if (c.blocks_per_sm < 0 || c.wait_cycles < 0) return set_error(TROUTE_EINVAL, "negative cfg field");
+    if (c.mapping < 0 || c.mapping > 3) return set_error(TROUTE_EINVAL, "cfg.mapping must be 0..3");
     return TROUTE_OK;
 }
 
@@ -178,13 +179,17 @@ struct troute_handle {
     DBuf<int> qcol, nseg, block_level, lb_ptr_d, up_ptr, up_idx, down, done, step_base;
     DBuf<double> qscale, q, d, v, ring, tmp, qlat_buf, hist;
     DBuf<long long> tile_off, seg_map_d, reach_map_d;
-    DBuf<unsigned long long> wave_ptr, ticket;
+    DBuf<unsigned long long> wave_ptr, ticket, rq_ctr;
+    DBuf<int> df_cnt;
+    DBuf<int2> df_rq, df_heads;
+    DBuf<double> df_rh;
+    int n_heads = 0, R_real = 0;
     DBuf<DevStats> stats;
     int hist_ts = 0;
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    int grid = 0, threads = 128;
+    int grid = 0, threads = 128, mapping = 2;
     int last_n_ts = 0;
 
     cudaGraph_t graph = nullptr;
@@ -226,6 +231,7 @@ struct troute_handle {
         qscale.release(); q.release(); d.release(); v.release(); ring.release(); tmp.release();
         qlat_buf.release(); hist.release(); tile_off.release(); seg_map_d.release();
         reach_map_d.release(); wave_ptr.release(); ticket.release(); stats.release();
+        rq_ctr.release(); df_cnt.release(); df_rq.release(); df_heads.release(); df_rh.release();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -240,6 +246,29 @@ static int upload(DBuf<T>& b, const std::vector<T>& h, cudaStream_t s)
     if (h.empty()) return TROUTE_OK;
     return cuda_check(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s),
                       "upload");
+}
+
+// Persistent grid sized by occupancy: SMs x resident blocks per SM (capped by
+// cfg.blocks_per_sm). Mapping 2 (per-lane refill) always runs 128-thread blocks.
+static int launch_shape(troute_handle* H)
+{
+    int rc, dev = 0, sms = 0, bps = 0;
+    if ((rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
+    if ((rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr"))) return rc;
+    H->mapping = H->cfg.mapping ? H->cfg.mapping : 3;
+    if (H->mapping == 3) {
+        H->threads = 128;
+        if ((rc = route_dataflow_occupancy(&bps))) return rc;
+    } else if (H->mapping == 2) {
+        H->threads = 128;
+        if ((rc = route_pool_occupancy(&bps))) return rc;
+    } else {
+        H->threads = H->cfg.threads_per_block ? H->cfg.threads_per_block : 128;
+        if ((rc = route_occupancy(H->threads, &bps))) return rc;
+    }
+    if (H->cfg.blocks_per_sm > 0) bps = std::min(bps, H->cfg.blocks_per_sm);
+    H->grid = std::max(1, sms * std::max(1, bps));
+    return TROUTE_OK;
 }
 
 // Builds the device schedule for a forest and uploads everything.
@@ -329,6 +358,16 @@ static int build_handle(troute_handle* H, const Forest& f, const std::vector<tro
         }
     }
 
+    // items ready at the start of a run: reaches without upstream reaches, step 0
+    {
+        std::vector<int2> heads;
+        for (int ri = 0; ri < H->R_int; ++ri)
+            if (nseg[ri] >= 0 && up_ptr[ri + 1] == up_ptr[ri]) heads.push_back(int2{ri, 0});
+        H->n_heads = (int)heads.size();
+        H->R_real = R;
+        if ((rc = upload(H->df_heads, heads.empty() ? std::vector<int2>{int2{0, 0}} : heads, H->stream))) return rc;
+    }
+
     // parameters in tile order
     std::vector<double2> planes[kParamPlanes];
     for (auto& p : planes) p.assign(H->S_int, double2{0.0, 0.0});
@@ -374,14 +413,7 @@ static int build_handle(troute_handle* H, const Forest& f, const std::vector<tro
     if ((rc = cuda_check(cudaMemsetAsync(H->done.p, 0, H->done.n * sizeof(int), st), "memset"))) return rc;
     if ((rc = cuda_check(cudaMemsetAsync(H->step_base.p, 0, sizeof(int), st), "memset"))) return rc;
 
-    // launch shape: persistent grid, occupancy-sized
-    int dev = 0, sms = 0, bps = 0;
-    if ((rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
-    if ((rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr"))) return rc;
-    H->threads = H->cfg.threads_per_block ? H->cfg.threads_per_block : 128;
-    if ((rc = route_occupancy(H->threads, &bps))) return rc;
-    if (H->cfg.blocks_per_sm > 0) bps = std::min(bps, H->cfg.blocks_per_sm);
-    H->grid = std::max(1, sms * std::max(1, bps));
+    if ((rc = launch_shape(H))) return rc;
     return cuda_check(cudaStreamSynchronize(st), "build sync");
 }
 
@@ -501,18 +533,8 @@ extern "C" int troute_set_cfg(troute_handle* h, const troute_cfg* cfg)
     if (!h || !cfg) return set_error(TROUTE_EINVAL, "null argument");
     int rc = check_cfg(*cfg);
     if (rc) return rc;
-    const bool shape = cfg->threads_per_block != h->cfg.threads_per_block || cfg->blocks_per_sm != h->cfg.blocks_per_sm;
     h->cfg = *cfg;
-    if (shape) {
-        int dev = 0, sms = 0, bps = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        h->threads = cfg->threads_per_block ? cfg->threads_per_block : 128;
-        if ((rc = route_occupancy(h->threads, &bps))) return rc;
-        if (cfg->blocks_per_sm > 0) bps = std::min(bps, cfg->blocks_per_sm);
-        h->grid = std::max(1, sms * std::max(1, bps));
-    }
-    return TROUTE_OK;
+    return launch_shape(h);
 }
 
 extern "C" int troute_info(const troute_handle* h, int* n_reaches, int* n_segments, int* n_levels,
@@ -637,7 +659,24 @@ static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, cudaS
     if ((rc = cuda_check(cudaMemsetAsync(H->ticket.p, 0, sizeof(unsigned long long), st), "memset"))) return rc;
     if ((rc = cuda_check(cudaMemsetAsync(H->stats.p, 0, sizeof(DevStats), st), "memset"))) return rc;
     if (timed && (rc = cuda_check(cudaEventRecord(H->ev0, st), "event"))) return rc;
-    if ((rc = launch_route(H->net(), run, H->grid, H->threads, st))) return rc;
+    if (H->mapping == 3) {
+        DataflowDev df;
+        df.cnt = H->df_cnt.p;
+        df.rq = H->df_rq.p;
+        df.rq_head = H->rq_ctr.p;
+        df.rq_tail = H->rq_ctr.p + 1;
+        df.rh = H->df_rh.p;
+        df.heads = H->df_heads.p;
+        df.n_heads = H->n_heads;
+        df.n_items = (unsigned long long)H->R_real * (unsigned long long)n_ts;
+        rc = launch_route_dataflow(H->net(), run, df, H->grid, st);
+    } else if (H->mapping == 2) {
+        rc = launch_route_pool(H->net(), run, H->grid, H->threads, st);
+    } else {
+        rc = launch_route(H->net(), run, H->grid, H->threads, st);
+    }
+    if (rc) return rc;
+    if (H->mapping >= 2 && (rc = launch_velocity(H->net(), st))) return rc;
     if (timed && (rc = cuda_check(cudaEventRecord(H->ev1, st), "event"))) return rc;
     return launch_bump_steps(H->step_base.p, n_ts, st);
 }
@@ -654,6 +693,12 @@ static int prepare_run(troute_handle* H, int n_ts)
     if (H->cfg.record_history) {
         if ((rc = H->hist.alloc((size_t)n_ts * H->S_int))) return rc;
         H->hist_ts = n_ts;
+    }
+    if (H->mapping == 3) {
+        const size_t R = (size_t)std::max(1, H->R_int);
+        if ((rc = H->df_cnt.alloc((size_t)n_ts * R)) || (rc = H->df_rh.alloc((size_t)(n_ts + 1) * R)) ||
+            (rc = H->df_rq.alloc(std::max<size_t>(1, (size_t)H->R_real * (size_t)n_ts))) || (rc = H->rq_ctr.alloc(2)))
+            return rc;
     }
     return cuda_check(cudaStreamSynchronize(H->stream), "wave sync");
 }
@@ -672,6 +717,10 @@ static int collect(troute_handle* H, troute_stats* stats, bool timed)
         stats->warm_used = ds.warm_used;
         stats->warm_fallback = ds.warm_fallback;
         for (int i = 0; i < 16; ++i) stats->iter_hist[i] = ds.hist[i];
+        stats->warp_passes = ds.warp_passes;
+        stats->lane_busy = ds.lane_busy;
+        stats->lane_wait = ds.lane_wait;
+        stats->lane_idle = ds.lane_idle;
         stats->timeout = ds.error == TROUTE_ETIMEOUT;
         if (timed) {
             float ms = 0.f;

@@ -67,6 +67,7 @@ TR_HD inline SegP derive_seg(const troute_chparams& c)
 struct DevStats {
     unsigned long long solves, iterations, retries, early_exits, warm_used, warm_fallback;
     unsigned long long hist[16];
+    unsigned long long warp_passes, lane_busy, lane_wait, lane_idle;
     int error;       // 0 ok, TROUTE_ETIMEOUT, TROUTE_EINVAL (bad index seen)
     int err_reach;   // internal reach of the first failure
     int err_step;    // step of the first failure
@@ -114,6 +115,18 @@ struct RunDev {
     double* q_hist;          // optional [n_ts][n_seg_int]
 };
 
+// Ready-queue state of one run of the dataflow kernel (mapping 3).
+struct DataflowDev {
+    int* cnt;                       // [n_ts][n_reach_int] completed dependencies
+    int2* rq;                       // [n_items] ready (reach, step) items
+    unsigned long long* rq_head;    // claimed slots
+    unsigned long long* rq_tail;    // written slots
+    double* rh;                     // [n_ts + 1][n_reach_int] reach outflow per step
+    const int2* heads;              // (headwater reach, 0) items, ready at the start
+    int n_heads;
+    unsigned long long n_items;     // real reaches x n_ts
+};
+
 // Launch helpers implemented in kernels.cu (all asynchronous on `stream`).
 int launch_reach_parallel(const troute_chparams* p, const double* ql, const int* rs,
                           const int* rl, const double* qu, const double* qd, const double* dp,
@@ -122,6 +135,10 @@ int launch_reach_parallel(const troute_chparams* p, const double* ql, const int*
                           void* stream);
 int launch_route(const NetDev& net, const RunDev& run, int grid, int threads, void* stream);
 int route_occupancy(int threads, int* blocks_per_sm);
+int launch_route_pool(const NetDev& net, const RunDev& run, int grid, int threads, void* stream);
+int route_pool_occupancy(int* blocks_per_sm);
+int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, int grid, void* stream);
+int route_dataflow_occupancy(int* blocks_per_sm);
 int launch_bump_steps(int* step_base, int n_ts, void* stream);
 int launch_fill_int(int* p, long long n, const int* value_dev, int value_host, void* stream);
 int launch_scatter(const double* src, const long long* map, long long n, double* dst,
@@ -129,5 +146,7 @@ int launch_scatter(const double* src, const long long* map, long long n, double*
 int launch_gather(const double* src, const long long* map, long long n, double* dst,
                   void* stream);
 int launch_timeout_probe(DevStats* stats, long long wait_cycles, void* stream);
+int launch_debug_pow(const double* x, int n, double* out, void* stream);
+int launch_velocity(const NetDev& net, void* stream);
 
 }  // namespace tr

@@ -1,4 +1,5 @@
 """GB300-native Muskingum-Cunge secant routing (t-route MC path) over a C ABI."""
 from .api import (  # noqa: F401
     CHPARAMS_DTYPE, CHPARAMS_F32_DTYPE, Cfg, Network, Stats, TrouteError, device_info, exported_symbols, levels,
-    lib, library_path, make_cfg, mc_reach_parallel, route_tree, validate, wavefront_fp64)
+    debug_pow, lib, library_path, make_cfg, mc_reach_parallel, route_tree, timeout_probe, validate,
+    wavefront_fp64)

@@ -57,7 +57,8 @@ class Cfg(C.Structure):
         ("warm_start", C.c_int),
         ("warm_k", C.c_int),
         ("record_history", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("mapping", C.c_int),
+        ("reserved", C.c_int * 6),
     ]
 
 
@@ -70,6 +71,10 @@ class Stats(C.Structure):
         ("warm_used", C.c_ulonglong),
         ("warm_fallback", C.c_ulonglong),
         ("iter_hist", C.c_ulonglong * 16),
+        ("warp_passes", C.c_ulonglong),
+        ("lane_busy", C.c_ulonglong),
+        ("lane_wait", C.c_ulonglong),
+        ("lane_idle", C.c_ulonglong),
         ("kernel_ms", C.c_double),
         ("timeout", C.c_int),
         ("reserved", C.c_int * 3),
@@ -84,6 +89,10 @@ class Stats(C.Structure):
             "warm_used": int(self.warm_used),
             "warm_fallback": int(self.warm_fallback),
             "iter_hist": [int(x) for x in self.iter_hist],
+            "warp_passes": int(self.warp_passes),
+            "lane_busy": int(self.lane_busy),
+            "lane_wait": int(self.lane_wait),
+            "lane_idle": int(self.lane_idle),
             "kernel_ms": float(self.kernel_ms),
             "timeout": int(self.timeout),
         }
@@ -131,6 +140,7 @@ _SIGS = {
     "troute_checkpoint": ([_P, _P, _P], _I),
     "troute_restore": ([_P, _P, C.c_size_t], _I),
     "troute_debug_timeout_probe": ([C.c_longlong], _I),
+    "troute_debug_pow": ([_P, _I, _P], _I),
     "troute_levels": ([_I, _P, _P, _P, _P, _P, _P], _I),
     "troute_validate": ([_P], _I),
     "troute_gen_tree": ([_U64, _I, _I, _I, _P, _P, _P, _P], _I),
@@ -208,6 +218,15 @@ def make_cfg(rtol=0.01, atol=0.01, maxiter=100, attempts=5, **kw) -> Cfg:
 def timeout_probe(wait_cycles: int = 2_000_000) -> int:
     """Runs the bounded-wait probe kernel; returns the status code (ETIMEOUT expected)."""
     return lib().troute_debug_timeout_probe(int(wait_cycles))
+
+
+def debug_pow(x):
+    """Device evaluation of the solver's powers and CUDA's pow():
+    (ours_23, ours_53, cuda_23, cuda_53)."""
+    x = _f64(x)
+    out = np.zeros(4 * x.size)
+    _check(lib().troute_debug_pow(_ptr(x), int(x.size), _ptr(out)))
+    return tuple(out.reshape(4, -1))
 
 
 def device_info() -> dict:

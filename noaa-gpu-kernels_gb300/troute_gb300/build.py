@@ -22,7 +22,7 @@ INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu"]
+CU_SOURCES = ["kernels.cu", "route_pool.cu", "route_dataflow.cu"]
 CPP_SOURCES = ["network.cpp", "capi.cpp", "gen.cpp"]
 
 
@@ -61,10 +61,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cuda_inc = os.path.join(CUDA_HOME, "include")
     jobs = []
     objs = []
+    # No implicit FMA contraction: the solver then rounds every +, -, *, / like
+    # the reference's C on the host (explicit fma() calls are unaffected).
+    fmad = ["-fmad=false"] if os.environ.get("TROUTE_FMAD", "0") == "0" else []
     for f in CU_SOURCES:
         o = os.path.join(BUILD, f + ".o")
         objs.append(o)
-        jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xptxas", "-v",
+        jobs.append([NVCC, *ARCH, *fmad, "-O3", "-lineinfo", "-std=c++17", "-Xptxas", "-v",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE,
                      "-c", os.path.join(CSRC, f), "-o", o])
     for f in CPP_SOURCES:
@@ -82,7 +85,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.replace(tmp, LIB)
     # keep the ptxas report next to the objects (registers / spills per kernel)
     with open(os.path.join(BUILD, "ptxas.txt"), "w") as fh:
-        fh.write(logs[0])
+        fh.write("".join(logs[: len(CU_SOURCES)]))
     return LIB
 
 

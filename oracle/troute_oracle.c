@@ -28,6 +28,79 @@
 
 #define MINDEPTH 0.01 /* troute_mc_final.cu:58 */
 
+/* ---------------------------------------------------------------------------
+ * R^(2/3) and R^(5/3). Mode 0 calls the C library's pow() exactly as the
+ * reference does. Mode 1 returns the correctly rounded values instead, from
+ * this file's own evaluation of R^fl(2/3) and R^fl(5/3) (the exponents the
+ * reference passes are the doubles nearest 2/3 and 5/3): split R = y 2^(3k)
+ * with y in [1, 8) (frexp / ldexp, exact), z = cbrt(y)^2 to a few ulp, then
+ * one Newton correction delta = -(z^3 - y^2) / (3 z^2) with the residual
+ * formed from error-free products (a*b - fl(a*b) = fma(a, b, -fl(a*b))), the
+ * exponent offset as the factor 1 + (fl(2/3) - 2/3) ln R, and round
+ * z + (delta + z c2) and y z + (err(y z) + y delta + y z c5). Mode 1 is the platform-independent form of the
+ * same arithmetic; the GPU library uses the same definition, so the two can be
+ * compared bit for bit.
+ * ------------------------------------------------------------------------- */
+static int g_pow_mode = 0;
+/* fl(2/3) - 2/3 = -(1/3) 2^-53 and fl(5/3) - 5/3 = (1/3) 2^-52 */
+#define FL23_MINUS_23 (-3.700743415417188e-17)
+#define FL53_MINUS_53 (7.401486830834377e-17)
+
+void oracle_set_pow_mode(int mode) { g_pow_mode = mode; }
+
+static void cr_pow23_53(double x, double* p23, double* p53)
+{
+    if (!(x > 0.0) || isinf(x)) {
+        const double v = (x == 0.0 || isinf(x)) ? x : NAN;
+        *p23 = v;
+        *p53 = v;
+        return;
+    }
+    int e;
+    const double m = frexp(x, &e); /* x = m 2^e, m in [0.5, 1) */
+    const int e1 = e - 1;          /* x = (2m) 2^e1 */
+    const int k = (e1 >= 0) ? e1 / 3 : -((-e1 + 2) / 3);
+    const int j = e1 - 3 * k;
+    const double y = ldexp(2.0 * m, j); /* [1, 8) */
+    const double c = cbrt(y);
+    const double z = c * c;
+    const double p = z * z, pe = fma(z, z, -p);
+    const double q = z * p, qe = fma(z, p, -q);
+    const double t = z * pe;
+    const double s = y * y, se = fma(y, y, -s);
+    const double d = (q - s) + ((qe + t) - se);
+    const double delta = -d / (3.0 * p);
+    const double w0 = y * z, we = fma(y, z, -w0);
+    /* the reference's exponents are the doubles nearest 2/3 and 5/3, not the
+     * rationals: x^fl(2/3) = x^(2/3) (1 + e2 ln x), e2 = fl(2/3) - 2/3 */
+    const double L = log(x);
+    const double c2 = FL23_MINUS_23 * L, c5 = FL53_MINUS_53 * L;
+    *p23 = ldexp(z + (delta + z * c2), 2 * k);
+    *p53 = ldexp(w0 + ((we + y * delta) + w0 * c5), 5 * k);
+}
+
+static double P23(double x)
+{
+    if (g_pow_mode == 0) return pow(x, 2.0 / 3.0);
+    double a, b;
+    cr_pow23_53(x, &a, &b);
+    return a;
+}
+
+static double P53(double x)
+{
+    if (g_pow_mode == 0) return pow(x, 5.0 / 3.0);
+    double a, b;
+    cr_pow23_53(x, &a, &b);
+    return b;
+}
+
+void oracle_pow23_53(double x, double* p23, double* p53)
+{
+    *p23 = P23(x);
+    *p53 = P53(x);
+}
+
 /* Channel geometry at depth h: trapezoid plus compound (floodplain) channel.
  * troute_mc_final.cu:30-40 (inlined at :200-205 and :216-221). */
 typedef struct geo {
@@ -55,8 +128,8 @@ static void channel_geometry(double h, double bfd, double bw, double twcc, doubl
 static double celerity(double h, const geo* g, double s0, double n_ch, double bw, double z)
 {
     if (!(h > 0.0)) return 0.0;
-    double r23 = pow(g->R, 2.0 / 3.0);
-    double r53 = pow(g->R, 5.0 / 3.0);
+    double r23 = P23(g->R);
+    double r53 = P53(g->R);
     return fmax(0.0, (sqrt(s0) / n_ch) *
                          ((5.0 / 3.0) * r23 -
                           (2.0 / 3.0) * r53 * (2.0 * sqrt(1.0 + z * z) / (bw + 2.0 * h * z))));
@@ -67,7 +140,7 @@ static double manning_q(const geo* g, double n_ch, double ncc, double s0)
 {
     if (!(g->WP + g->WPC > 0.0)) return 0.0;
     return (1.0 / (((g->WP * n_ch) + (g->WPC * ncc)) / (g->WP + g->WPC))) * (g->A + g->AC) *
-           pow(g->R, 2.0 / 3.0) * sqrt(s0);
+           P23(g->R) * sqrt(s0);
 }
 
 double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
@@ -182,7 +255,7 @@ double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
     double Rv = (h * (bw + twl) / 2.0) /
                 (bw + 2.0 * sqrt(((twl - bw) / 2.0) * ((twl - bw) / 2.0) + h * h));
     if (Rv < 0.0) Rv = 0.0;
-    *velc = (1.0 / n_ch) * pow(Rv, 2.0 / 3.0) * sqrt(s0);
+    *velc = (1.0 / n_ch) * P23(Rv) * sqrt(s0);
     *depthc = h;
     *iters = total;
     return qdc;
@@ -229,6 +302,7 @@ typedef struct tree_job {
     const oracle_tol* tol;
     double *q[2], *d[2], *v, *rl[2];
     double* q_hist;
+    int* it_hist;
     int n_threads;
     pthread_barrier_t barrier;
 } tree_job;
@@ -266,6 +340,7 @@ static void route_reach(tree_job* J, int r, int t, long long* iters)
         J->d[cur][s] = dc;
         J->v[s] = vc;
         if (J->q_hist) J->q_hist[(size_t)t * (size_t)J->n_segments + s] = q;
+        if (J->it_hist) J->it_hist[(size_t)t * (size_t)J->n_segments + s] = it;
         quc_next = q;
         q_last = q;
         *iters += it;
@@ -302,6 +377,23 @@ int oracle_route_tree(const int* reach_seg_start, const int* reach_seg_len,
                       double* reach_last_out, double* q_hist,
                       long long* iters_total, int n_threads)
 {
+    return oracle_route_tree_it(reach_seg_start, reach_seg_len, reach_up_ptr, reach_up_idx, level_ptr,
+                                level_reach, n_reaches, n_levels, n_segments, params, qlat_ts, qdp0, dp0,
+                                reach_last0, n_ts, dt, tol, q_out, d_out, v_out, reach_last_out, q_hist,
+                                NULL, iters_total, n_threads);
+}
+
+int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
+                         const int* reach_up_ptr, const int* reach_up_idx,
+                         const int* level_ptr, const int* level_reach,
+                         int n_reaches, int n_levels, int n_segments,
+                         const oracle_chparams* params, const double* qlat_ts,
+                         const double* qdp0, const double* dp0, const double* reach_last0,
+                         int n_ts, double dt, const oracle_tol* tol,
+                         double* q_out, double* d_out, double* v_out,
+                         double* reach_last_out, double* q_hist, int* it_hist,
+                         long long* iters_total, int n_threads)
+{
     if (n_reaches < 0 || n_segments < 0 || n_levels < 0 || n_ts < 0) return 1;
     if (n_threads < 1) n_threads = 1;
     tree_job J;
@@ -321,6 +413,7 @@ int oracle_route_tree(const int* reach_seg_start, const int* reach_seg_len,
     J.dt = dt;
     J.tol = tol;
     J.q_hist = q_hist;
+    J.it_hist = it_hist;
     J.n_threads = n_threads;
     const size_t S = (size_t)n_segments, R = (size_t)n_reaches;
     double* buf = (double*)calloc(4 * S + 2 * R + 1, sizeof(double));

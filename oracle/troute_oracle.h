@@ -34,6 +34,12 @@ typedef struct oracle_tol {
     int attempts;
 } oracle_tol;
 
+/* Power function used for R^(2/3), R^(5/3): 0 = the C library's pow() (the
+ * reference's, default), 1 = correctly rounded values (platform independent).
+ * Process-wide; not thread-safe to change while routing. */
+void oracle_set_pow_mode(int mode);
+void oracle_pow23_53(double x, double* p23, double* p53);
+
 /* One segment solve (troute_mc_final.cu:42-139 / :181-248). Returns qdc and
  * writes depth, velocity and the number of secant iterations run. */
 double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
@@ -70,6 +76,19 @@ int oracle_route_tree(const int* reach_seg_start, const int* reach_seg_len,
                       double* q_out, double* d_out, double* v_out,
                       double* reach_last_out, double* q_hist,
                       long long* iters_total, int n_threads);
+
+/* Same, also writing the secant iterations of every solve to it_hist
+ * [n_ts][n_segments] (may be NULL). */
+int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
+                         const int* reach_up_ptr, const int* reach_up_idx,
+                         const int* level_ptr, const int* level_reach,
+                         int n_reaches, int n_levels, int n_segments,
+                         const oracle_chparams* params, const double* qlat_ts,
+                         const double* qdp0, const double* dp0, const double* reach_last0,
+                         int n_ts, double dt, const oracle_tol* tol,
+                         double* q_out, double* d_out, double* v_out,
+                         double* reach_last_out, double* q_hist, int* it_hist,
+                         long long* iters_total, int n_threads);
 
 #ifdef __cplusplus
 }

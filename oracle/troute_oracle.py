@@ -64,8 +64,34 @@ def oracle():
         L.oracle_route_tree.restype = C.c_int
         L.oracle_mc_solve.argtypes = [C.c_double] * 5 + [_P, C.c_double, _P, _P, _P, _P]
         L.oracle_mc_solve.restype = C.c_double
+        L.oracle_set_pow_mode.argtypes = [C.c_int]
+        L.oracle_set_pow_mode.restype = None
+        L.oracle_pow23_53.argtypes = [C.c_double, _P, _P]
+        L.oracle_pow23_53.restype = None
         _ORC = L
     return _ORC
+
+
+class pow_mode:
+    """Context manager: route the oracle's R^(2/3), R^(5/3) through the C
+    library's pow() (0, the reference's) or the correctly rounded form (1)."""
+
+    def __init__(self, mode: int):
+        self.mode = mode
+
+    def __enter__(self):
+        oracle().oracle_set_pow_mode(self.mode)
+        return self
+
+    def __exit__(self, *a):
+        oracle().oracle_set_pow_mode(0)
+
+
+def pow23_53(x: float, mode: int = 0):
+    a, b = C.c_double(), C.c_double()
+    with pow_mode(mode):
+        oracle().oracle_pow23_53(float(x), C.byref(a), C.byref(b))
+    return a.value, b.value
 
 
 def ref_available() -> bool:

@@ -1,14 +1,17 @@
 """GPU parity: the CUDA path through the C ABI against the oracle and the
 reference-made golden fixtures.
 
-Bars (relative error on discharge, and on depth / velocity where stated):
-  - reference tolerance (rtol = atol = 0.01): whole multi-step trajectories,
-    every step, 1e-10;
-  - rtol = 1e-8: one step at a time from a state both sides share, 1e-10.
-    (Multi-step trajectories at 1e-8 are not comparable below ~1e-4 by any
-    implementation that is not bit-identical to the host libm: the oracle
-    itself moves that much under a 1-ulp input change, see
-    test_oracle.py::test_tight_tolerance_trajectories_are_ulp_sensitive.)
+The solver's powers R^fl(2/3), R^fl(5/3) are correctly rounded on the device
+and the rest of its arithmetic is compiled without FMA contraction, so:
+  - against the oracle with correctly rounded powers (oracle pow mode 1) the
+    GPU is bit-identical: whole multi-step trajectories, every tolerance;
+  - against the reference's own routines and the oracle with the C library's
+    pow() (which misrounds ~0.1% of these powers by 1 ulp), discharge agrees
+    to 1e-10 relative over whole runs at the reference tolerance
+    (rtol = atol = 0.01). At rtol = 1e-8 the reference algorithm itself is
+    ulp-sensitive over many steps (test_oracle.py::
+    test_tight_tolerance_trajectories_are_ulp_sensitive), so there the libm
+    comparison is statistical.
 """
 import os
 
@@ -45,15 +48,33 @@ def test_reach_parallel_matches_reference_golden():
     assert rel_err(qo, g["qo"]) < REL
     assert rel_err(dpo, g["dpo"]) < REL
     assert rel_err(vo, g["vo"]) < REL
-    assert st["solves"] == len(qo) and st["early_exits"] >= 6
+    assert st["solves"] == len(qo) and st["early_exits"] >= 3
 
 
-def test_reach_parallel_tight_tolerance_matches_oracle():
+def test_reach_parallel_bit_identical_to_oracle():
     p, ql, rs, rl, qu, qd, dp = make_golden.cpu_mc_inputs()
-    a = O.cpu_mc(p, ql, rs, rl, qu, qd, dp, tol=TIGHT)
-    qo, vo, dpo, st = T.mc_reach_parallel(p, ql, rs, rl, qu, qd, dp, cfg=cfg_of(TIGHT), return_stats=True)
-    assert rel_err(qo, a[0]) < REL and rel_err(dpo, a[2]) < REL and rel_err(vo, a[1]) < REL
-    assert st["iterations"] == a[3]
+    for tol in (O.REF_TOL, TIGHT):
+        with O.pow_mode(1):
+            a = O.cpu_mc(p, ql, rs, rl, qu, qd, dp, tol=tol)
+        qo, vo, dpo, st = T.mc_reach_parallel(p, ql, rs, rl, qu, qd, dp, cfg=cfg_of(tol), return_stats=True)
+        np.testing.assert_array_equal(qo, a[0])
+        np.testing.assert_array_equal(vo, a[1])
+        np.testing.assert_array_equal(dpo, a[2])
+        assert st["iterations"] == a[3]
+
+
+def test_device_powers_are_correctly_rounded():
+    rng = np.random.default_rng(11)
+    x = np.concatenate([np.exp(rng.uniform(np.log(1e-6), np.log(1e4), 200000)),
+                        [0.0, 1.0, 8.0, 27.0, 0.125, 1e-310, 1e300, 5e-324]])
+    o23, o53, c23, c53 = T.debug_pow(x)
+    r23 = np.array([O.pow23_53(v, mode=1)[0] for v in x])
+    r53 = np.array([O.pow23_53(v, mode=1)[1] for v in x])
+    np.testing.assert_array_equal(o23, r23)
+    np.testing.assert_array_equal(o53, r53)
+    # against CUDA's pow() (documented max error 2 ulp): within 2 ulp everywhere
+    ulp = lambda a, b: np.abs(a.view(np.int64) - b.view(np.int64))
+    assert ulp(o23, c23).max() <= 2 and ulp(o53, c53).max() <= 2
 
 
 # ---------------------------------------------------------------- tree, reference tolerance
@@ -80,24 +101,18 @@ def test_tree_full_history_matches_oracle_reference_tol():
     assert g["stats"]["iterations"] == o["iterations"]
 
 
-# ---------------------------------------------------------------- tree, tight tolerance
-def _oracle_state(c, t, tol):
-    """Oracle state after t steps: (q, d, reach_last)."""
-    if t == 0:
-        return c["q0"], c["d0"], c["rl0"]
-    o = O.route_tree(c["topo"], c["params"], c["qlat"][:t], c["q0"], c["d0"], c["rl0"], tol=tol)
-    return o["q"], o["d"], o["reach_last"]
-
-
-@pytest.mark.parametrize("t", [0, 5, 60, 287])
-def test_tree_one_step_tight_tolerance_matches_oracle(t):
+# ---------------------------------------------------------------- tree, bit-identical
+@pytest.mark.parametrize("tol", [O.REF_TOL, TIGHT], ids=["ref_tol", "rtol_1e-8"])
+def test_tree_full_history_bit_identical_to_oracle(tol):
     c = synth.network("c0")
-    q, d, rl = _oracle_state(c, t, TIGHT)
-    o = O.route_tree(c["topo"], c["params"], c["qlat"][t:t + 1], q, d, rl, tol=TIGHT)
-    g = T.route_tree(c["topo"], c["params"], c["qlat"][t:t + 1], q, d, rl, cfg=cfg_of(TIGHT))
-    assert rel_err(g["q"], o["q"]) < REL
-    assert rel_err(g["d"], o["d"]) < REL
-    assert rel_err(g["v"], o["v"]) < REL
+    args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    with O.pow_mode(1):
+        o = O.route_tree(*args, tol=tol, history=True)
+    g = T.route_tree(*args, cfg=cfg_of(tol), history=True)
+    np.testing.assert_array_equal(g["q_hist"], o["q_hist"])
+    for k in ("q", "d", "v", "reach_last"):
+        np.testing.assert_array_equal(g[k], o[k])
+    assert g["stats"]["iterations"] == o["iterations"]
 
 
 def test_tree_tight_tolerance_trajectory_statistics():
@@ -115,7 +130,7 @@ def test_tree_tight_tolerance_trajectory_statistics():
 def _topo(seg_len, ups):
     seg_len = np.asarray(seg_len, np.int32)
     return {"n_segments": int(seg_len.sum()),
-            "reach_seg_start": np.concatenate([[0], np.cumsum(seg_len)[:-1]]).astype(np.int32),
+            "reach_seg_start": (np.cumsum(seg_len) - seg_len).astype(np.int32),
             "reach_seg_len": seg_len,
             "reach_up_ptr": np.concatenate([[0], np.cumsum([len(u) for u in ups])]).astype(np.int32),
             "reach_up_idx": np.array([x for u in ups for x in u], np.int32)}
@@ -220,13 +235,19 @@ def test_checkpoint_resume_is_bit_identical():
 
 
 def test_launch_shape_does_not_change_results():
+    """The schedule (grid size, block shape, reach-to-warp mapping, which lane
+    takes which reach) is not part of the arithmetic: identical bits for all."""
     c = synth.network("tree:20000", seed=8, n_ts=16)
-    outs = []
-    for tpb, bps in ((128, 0), (64, 1), (32, 2)):
-        cfg = T.make_cfg(threads_per_block=tpb, blocks_per_sm=bps)
-        outs.append(T.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"], cfg=cfg)["q"])
-    for x in outs[1:]:
-        np.testing.assert_array_equal(x, outs[0])
+    args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    ref = None
+    for mapping, shapes in ((3, ((0, 0), (128, 1), (128, 2))), (2, ((0, 0), (128, 1))),
+                            (1, ((128, 0), (64, 1), (32, 2)))):
+        outs = [T.route_tree(*args, cfg=T.make_cfg(mapping=mapping, threads_per_block=tpb, blocks_per_sm=bps))["q"]
+                for tpb, bps in shapes]
+        if ref is None:
+            ref = outs[0]
+        for x in outs:
+            np.testing.assert_array_equal(x, ref)
 
 
 def test_bounded_wait_times_out_cleanly():

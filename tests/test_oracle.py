@@ -146,3 +146,33 @@ def test_planted_mistake_is_caught():
                      tol=(1e-8, 1e-10, 100, 5))
     rel = np.abs(a["q"] - b["q"]) / np.maximum(np.abs(a["q"]), 1e-300)
     assert rel.max() > 1e-10
+
+
+def test_correctly_rounded_powers_against_libm_and_mpmath():
+    """Pow mode 1 gives the correctly rounded R^fl(2/3), R^fl(5/3); the C
+    library's pow() agrees except for rare 1-ulp misroundings."""
+    rng = np.random.default_rng(3)
+    xs = np.exp(rng.uniform(np.log(1e-4), np.log(1e3), 20000))
+    a = np.array([O.pow23_53(x, 0) for x in xs])
+    b = np.array([O.pow23_53(x, 1) for x in xs])
+    ulp = np.abs(a.view(np.int64) - b.view(np.int64))
+    assert ulp.max() <= 1 and (ulp > 0).mean() < 0.005
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.prec = 200
+    e2, e5 = mpmath.mpf(2.0 / 3.0), mpmath.mpf(5.0 / 3.0)
+    for x, (p23, p53) in zip(xs[:2000], b[:2000]):
+        assert p23 == float(mpmath.mpf(x) ** e2) and p53 == float(mpmath.mpf(x) ** e5)
+
+
+def test_pow_mode_changes_nothing_at_reference_tolerance():
+    """The correctly rounded powers change whole 288-step runs at the
+    reference tolerance by far less than the 1e-10 parity bar."""
+    from troute_gb300 import synth
+
+    c = synth.network("c0")
+    args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    a = O.route_tree(*args, history=True)
+    with O.pow_mode(1):
+        b = O.route_tree(*args, history=True)
+    rel = np.abs(a["q_hist"] - b["q_hist"]) / np.maximum(np.abs(a["q_hist"]), 1e-300)
+    assert rel.max() < 1e-10
