@@ -56,7 +56,7 @@ typedef struct troute_cfg {
     int attempts;           /* bracket-widening attempts */
     int threads_per_block;  /* 0: autotuned / default */
     int blocks_per_sm;      /* 0: occupancy-derived */
-    long long wait_cycles;  /* bound on each device-side wait, SM clocks; 0: ~2 s */
+    long long wait_cycles;  /* bound on each device-side wait without progress, SM clocks; 0: ~4 s */
     int warm_start;         /* 1: learned warm start (needs troute_set_warm_start) */
     int warm_k;             /* iterations a warm-started solve gets before the plain solve */
     int record_history;     /* 1: keep per-step discharge of every segment (troute_get_history) */

@@ -29,6 +29,7 @@ struct Lane {
     int ri, tau, g, ns, i, ub, ue, dn;
     long long base;        // tile slot of segment 0
     long long wait_t0;
+    unsigned long long wait_tail;  // queue tail seen when the current wait budget began
     double qup_head, quc_head, q_up_old, q_up_new, q_last;
     // current segment
     long long s;

@@ -653,7 +653,7 @@ static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, cudaS
     run.n_tickets = wp.back();
     run.ticket = H->ticket.p;
     run.stats = H->stats.p;
-    run.wait_cycles = H->cfg.wait_cycles > 0 ? H->cfg.wait_cycles : 4000000000LL;
+    run.wait_cycles = H->cfg.wait_cycles > 0 ? H->cfg.wait_cycles : 8000000000LL;
     run.tol = make_tol(H->cfg);
     run.q_hist = (H->cfg.record_history && H->hist.p) ? H->hist.p : nullptr;
     if ((rc = cuda_check(cudaMemsetAsync(H->ticket.p, 0, sizeof(unsigned long long), st), "memset"))) return rc;
@@ -665,9 +665,11 @@ static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, cudaS
         df.rq = H->df_rq.p;
         df.rq_head = H->rq_ctr.p;
         df.rq_tail = H->rq_ctr.p + 1;
+        df.n_done = H->rq_ctr.p + 2;
         df.rh = H->df_rh.p;
         df.heads = H->df_heads.p;
         df.n_heads = H->n_heads;
+        df.continue_items = H->cfg.reserved[0] & 1;
         df.n_items = (unsigned long long)H->R_real * (unsigned long long)n_ts;
         rc = launch_route_dataflow(H->net(), run, df, H->grid, st);
     } else if (H->mapping == 2) {
@@ -697,7 +699,7 @@ static int prepare_run(troute_handle* H, int n_ts)
     if (H->mapping == 3) {
         const size_t R = (size_t)std::max(1, H->R_int);
         if ((rc = H->df_cnt.alloc((size_t)n_ts * R)) || (rc = H->df_rh.alloc((size_t)(n_ts + 1) * R)) ||
-            (rc = H->df_rq.alloc(std::max<size_t>(1, (size_t)H->R_real * (size_t)n_ts))) || (rc = H->rq_ctr.alloc(2)))
+            (rc = H->df_rq.alloc(std::max<size_t>(1, (size_t)H->R_real * (size_t)n_ts))) || (rc = H->rq_ctr.alloc(3)))
             return rc;
     }
     return cuda_check(cudaStreamSynchronize(H->stream), "wave sync");

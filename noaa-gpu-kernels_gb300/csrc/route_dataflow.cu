@@ -12,17 +12,20 @@
 //
 //   cnt[t][r]   dependencies of (r, t) completed so far; (r, t) is ready at
 //               n_up(r) + (t > 0)
-//   rq[i]       ready items in the order they became ready; slot i is claimed
-//               by an idle lane (atomic head) before or after it is written
-//               (atomic tail); -1 = not yet written
+//   rq[i]       ready items in the order they became ready (atomic tail);
+//               idle lanes claim slots (atomic head); -1 = not yet written
 //   rh[t+1][r]  outflow of reach r at step t of this run, rh[0][r] the
 //               outflow of the step before the run (from the 4-slot ring of
 //               the handle's state); a whole run is kept, so upstream reaches
 //               never wait for downstream ones to consume a value.
-// Every item is pushed exactly once, so the queue ends with exactly n_items
-// entries and a claimed slot is always filled eventually. The head sums at a
-// reach use the upstream order of the reference (wavefront_mc.cu:525-531),
-// and the solve is lane_solver.cuh's, i.e. the reference's arithmetic.
+// The lane that makes an item ready continues with it itself when it has no
+// other work (the downstream item when two became ready), so busy lanes stay
+// in their warps and the queue carries only the rest. A warp claims only
+// slots that are already written (or that a racing warp is about to see
+// written); the run ends when the count of completed items reaches n_items.
+// The head sums at a reach use the upstream order of the reference
+// (wavefront_mc.cu:525-531), and the solve is lane_solver.cuh's, i.e. the
+// reference's arithmetic.
 #include "lane_solver.cuh"
 
 namespace tr {
@@ -30,6 +33,8 @@ namespace tr {
 namespace {
 constexpr unsigned kFullMask = 0xffffffffu;
 constexpr int L_FETCH = L_WAIT;  // claimed a queue slot, waiting for it to be written
+constexpr unsigned long long kWakeItems = 16;  // queued items that wake an idle warp
+constexpr long long kWakeCycles = 8000;        // ... or this long unclaimed (~4 us)
 
 __device__ __forceinline__ unsigned lanemask_lt_df()
 {
@@ -42,7 +47,56 @@ __device__ __forceinline__ long long ld_volatile_ll(const long long* p)
 {
     return *reinterpret_cast<const volatile long long*>(p);
 }
+
+__device__ __forceinline__ unsigned long long ld_volatile_ull(const unsigned long long* p)
+{
+    return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
 }  // namespace
+
+// Loads the reach head inflows of (ri, tau) (all its dependencies are
+// complete) and starts its first segment.
+__device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base, const NetDev& net,
+                                           const RunDev& run, const DataflowDev& df, LocalStats& ls,
+                                           unsigned int* hist_s)
+{
+    const int R = net.n_reach_int;
+#ifdef TROUTE_CHECK
+    // self-check build (the outflow history is NaN-filled before the run):
+    // every value (ri, tau) reads must already be written, and its own output
+    // slot must not be
+    {
+        bool ok = !isnan(__ldcg(df.rh + (size_t)tau * R + ri)) && isnan(__ldcg(df.rh + (size_t)(tau + 1) * R + ri));
+        for (int j = __ldg(net.up_ptr + ri); j < __ldg(net.up_ptr + ri + 1); ++j) {
+            const int u = __ldg(net.up_idx + j);
+            ok = ok && !isnan(__ldcg(df.rh + (size_t)tau * R + u)) && !isnan(__ldcg(df.rh + (size_t)(tau + 1) * R + u));
+        }
+        if (!ok) record_error(run.stats, TROUTE_EINVAL, ri, t_base + tau, 7);
+    }
+#endif
+    L.ri = ri;
+    L.tau = tau;
+    L.g = t_base + tau;
+    L.ns = __ldg(net.nseg + ri);
+    L.ub = __ldg(net.up_ptr + ri);
+    L.ue = __ldg(net.up_ptr + ri + 1);
+    L.dn = __ldg(net.down + ri);
+    L.base = __ldg(net.tile_off + ri / kLanes) + (ri % kLanes);
+    const double* rprev = df.rh + (size_t)tau * R;
+    const double* rcur = df.rh + (size_t)(tau + 1) * R;
+    L.qup_head = 0.0;
+    L.quc_head = 0.0;
+    for (int j = L.ub; j < L.ue; ++j) {
+        const int u = __ldg(net.up_idx + j);
+        L.qup_head += __ldcg(rprev + u);
+        L.quc_head += __ldcg(rcur + u);
+    }
+    L.q_up_old = 0.0;
+    L.q_up_new = 0.0;
+    L.q_last = 0.0;
+    L.i = 0;
+    L.mode = begin_segment(L, net, run, ls, hist_s) ? L_SOLVE : L_DONE;
+}
 
 __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df)
 {
@@ -55,38 +109,73 @@ __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev 
     const int t_base = __ldg(run.step_base);
     const int T = run.n_ts;
     const int R = net.n_reach_int;
-    bool exhausted = false;
     bool failed = false;
     unsigned long long slot = 0;
+    long long queued_since = -1;  // lane 0: when this idle warp first saw unclaimed items
     Lane L;
     L.mode = L_IDLE;
     unsigned long long n_pass = 0, n_busy = 0, n_wait = 0, n_idle = 0;
 
     while (true) {
         // ---- idle lanes claim queue slots (one atomic per warp) ----
+        // A warp claims only as many slots as there are queued items it could
+        // take (tail - head), so the ready work lands on few, full warps instead
+        // of one lane in each of many warps (a warp pays for every FP64
+        // instruction whatever the number of its busy lanes). Two warps can
+        // race past the tail; their extra lanes wait for the next items.
         const unsigned idle = __ballot_sync(kFullMask, L.mode == L_IDLE);
-        if (idle && !exhausted) {
-            const unsigned n = __popc(idle);
+        if (idle) {
+            // a warp with busy lanes tops itself up with whatever is queued; a
+            // warp with none waits until enough is queued to fill a good part
+            // of it, or until queued items have not been taken for a while
+            const bool has_busy = idle != kFullMask;
+            unsigned n = 0;
             unsigned long long base = 0;
             int err = 0;
             if (lane == 0) {
-                base = atomicAdd(df.rq_head, (unsigned long long)n);
+                const unsigned long long tail = ld_volatile_ull(df.rq_tail);
+                const unsigned long long head = ld_volatile_ull(df.rq_head);
                 err = ld_volatile_int(&run.stats->error);
+                if (tail > head) {
+                    const unsigned long long avail = tail - head;
+                    bool take = has_busy || avail >= kWakeItems;
+                    if (!take) {
+                        const long long now = clock64();
+                        if (queued_since < 0) queued_since = now;
+                        take = now - queued_since > kWakeCycles;
+                    }
+                    if (take) {
+                        queued_since = -1;
+                        n = (unsigned)min((unsigned long long)__popc(idle), avail);
+                        base = atomicAdd(df.rq_head, (unsigned long long)n);
+                    }
+                } else {
+                    queued_since = -1;
+                }
             }
+            n = __shfl_sync(kFullMask, n, 0);
             base = __shfl_sync(kFullMask, base, 0);
             err = __shfl_sync(kFullMask, err, 0);
             if (err) break;
-            if (base + n >= df.n_items) exhausted = true;
-            if (L.mode == L_IDLE) {
-                const unsigned long long my = base + __popc(idle & lt);
-                if (my < df.n_items) {
-                    slot = my;
+            if (n && L.mode == L_IDLE) {
+                const unsigned rank = __popc(idle & lt);
+                // racing warps can push the head past the end of the queue;
+                // such slots do not exist and are never read
+                if (rank < n && base + rank < df.n_items) {
+                    slot = base + rank;
                     L.mode = L_FETCH;
                     L.wait_t0 = clock64();
+                    L.wait_tail = 0;
                 }
             }
         }
-        if (__ballot_sync(kFullMask, L.mode != L_IDLE) == 0 && exhausted) break;
+        // the run is over once every (reach, step) item has completed; lanes
+        // still holding a claimed slot then leave it (it will not be written)
+        if (__ballot_sync(kFullMask, L.mode >= L_SOLVE) == 0) {
+            unsigned long long nd = 0;
+            if (lane == 0) nd = ld_volatile_ull(df.n_done);
+            if (__shfl_sync(kFullMask, nd, 0) >= df.n_items) break;
+        }
         {
             const unsigned wmask = __ballot_sync(kFullMask, L.mode == L_FETCH);
             const unsigned bmask = __ballot_sync(kFullMask, L.mode >= L_SOLVE);
@@ -100,33 +189,26 @@ __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev 
         if (L.mode == L_FETCH) {
             const long long raw = ld_volatile_ll(reinterpret_cast<const long long*>(df.rq + slot));
             const int ri = (int)(raw & 0xffffffffll);
-            if (ri >= 0) {
-                __threadfence();  // the item's inputs were published before it was queued
-                L.ri = ri;
-                L.tau = (int)(raw >> 32);
-                L.g = t_base + L.tau;
-                L.ns = __ldg(net.nseg + L.ri);
-                L.ub = __ldg(net.up_ptr + L.ri);
-                L.ue = __ldg(net.up_ptr + L.ri + 1);
-                L.dn = __ldg(net.down + L.ri);
-                L.base = __ldg(net.tile_off + L.ri / kLanes) + (L.ri % kLanes);
-                const double* rprev = df.rh + (size_t)L.tau * R;
-                const double* rcur = df.rh + (size_t)(L.tau + 1) * R;
-                L.qup_head = 0.0;
-                L.quc_head = 0.0;
-                for (int j = L.ub; j < L.ue; ++j) {
-                    const int u = __ldg(net.up_idx + j);
-                    L.qup_head += __ldcg(rprev + u);
-                    L.quc_head += __ldcg(rcur + u);
-                }
-                L.q_up_old = 0.0;
-                L.q_up_new = 0.0;
-                L.q_last = 0.0;
-                L.i = 0;
-                L.mode = begin_segment(L, net, run, ls, hist_s) ? L_SOLVE : L_DONE;
-            } else if (clock64() - L.wait_t0 > run.wait_cycles) {
-                record_error(run.stats, TROUTE_ETIMEOUT, -1, (int)(slot & 0x7fffffff), 6);
+            const int tau = (int)(raw >> 32);
+            if (ri >= 0 && (ri >= R || tau < 0 || tau >= T)) {
+                // an entry that names no item of this run: report, never index with it
+                record_error(run.stats, TROUTE_EINVAL, ri, tau, 8);
                 failed = true;
+            } else if (ri >= 0) {
+                __threadfence();  // the item's inputs were published before it was queued
+                start_item(L, ri, tau, t_base, net, run, df, ls, hist_s);
+            } else if (clock64() - L.wait_t0 > run.wait_cycles) {
+                // a slot can legitimately stay empty for long while the run
+                // advances; give up only if no item completed during a whole
+                // wait budget
+                const unsigned long long nd = ld_volatile_ull(df.n_done);
+                if (nd != L.wait_tail) {
+                    L.wait_tail = nd;
+                    L.wait_t0 = clock64();
+                } else {
+                    record_error(run.stats, TROUTE_ETIMEOUT, -1, (int)(slot & 0x7fffffff), 6);
+                    failed = true;
+                }
             }
         }
 
@@ -136,6 +218,8 @@ __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev 
         // ---- completed reaches: publish, count dependencies, queue ready items ----
         int npush = 0;
         int2 push0 = make_int2(-1, -1), push1 = make_int2(-1, -1);
+        const unsigned dmask = __ballot_sync(kFullMask, L.mode == L_DONE);
+        if (dmask && lane == 0) atomicAdd(df.n_done, (unsigned long long)__popc(dmask));
         if (L.mode == L_DONE) {
             __stcg(df.rh + (size_t)(L.tau + 1) * R + L.ri, L.q_last);
             __stcg(net.ring + (size_t)(L.g % kRing) * R + L.ri, L.q_last);
@@ -157,6 +241,17 @@ __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev 
                 }
             }
             L.mode = L_IDLE;
+            if (npush && df.continue_items) {
+                // continue with one newly ready item here (the downstream one when
+                // there are two: it lies toward the outlet); queue the other
+                __threadfence();  // other dependencies' writes, seen through the counters
+                const int2 mine = (npush == 2) ? push1 : push0;
+                if (npush == 2) push1 = make_int2(-1, -1);
+                --npush;
+                start_item(L, mine.x, mine.y, t_base, net, run, df, ls, hist_s);
+                // a reach without solve work completes at once; it is published
+                // in the next pass
+            }
         }
         // warp-aggregated append to the ready queue
         unsigned total = npush;
@@ -172,6 +267,12 @@ __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev 
             base = __shfl_sync(kFullMask, base, 31);
             const unsigned long long pos = base + (incl - npush);
             if (npush) __threadfence();  // every dependency's writes before the item is visible
+            if (npush && pos + npush > df.n_items) {
+                // more items than the run has: an accounting error, never write past the queue
+                record_error(run.stats, TROUTE_EINVAL, push0.x, push0.y, 9);
+                failed = true;
+                npush = 0;
+            }
             if (npush >= 1) {
                 const long long v = ((long long)push0.y << 32) | (unsigned)push0.x;
                 *reinterpret_cast<volatile long long*>(df.rq + pos) = v;
@@ -182,7 +283,7 @@ __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev 
             }
         }
         if (__any_sync(kFullMask, failed)) break;
-        if (__ballot_sync(kFullMask, L.mode >= L_SOLVE) == 0) __nanosleep(64);
+        if (__ballot_sync(kFullMask, L.mode >= L_SOLVE) == 0) __nanosleep(200);
     }
     if (lane == 0) {
         atomicAdd(&run.stats->warp_passes, n_pass);
@@ -205,6 +306,7 @@ __global__ void dataflow_init_kernel(NetDev net, RunDev run, DataflowDev df)
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *df.rq_head = 0;
         *df.rq_tail = (unsigned long long)df.n_heads;
+        *df.n_done = 0;
     }
 }
 
@@ -213,6 +315,10 @@ int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDe
     if (df.n_items == 0) return TROUTE_OK;
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e;
+#ifdef TROUTE_CHECK
+    if ((e = cudaMemsetAsync(df.rh, 0xff, (size_t)(run.n_ts + 1) * net.n_reach_int * sizeof(double), st)) != cudaSuccess)
+        return set_error(TROUTE_ECUDA, "dataflow set-up: %s", cudaGetErrorString(e));
+#endif
     if ((e = cudaMemsetAsync(df.cnt, 0, (size_t)run.n_ts * net.n_reach_int * sizeof(int), st)) != cudaSuccess ||
         (e = cudaMemsetAsync(df.rq, 0xff, (size_t)df.n_items * sizeof(int2), st)) != cudaSuccess ||
         (e = cudaMemcpyAsync(df.rq, df.heads, (size_t)df.n_heads * sizeof(int2), cudaMemcpyDeviceToDevice, st)) != cudaSuccess)

@@ -121,9 +121,11 @@ struct DataflowDev {
     int2* rq;                       // [n_items] ready (reach, step) items
     unsigned long long* rq_head;    // claimed slots
     unsigned long long* rq_tail;    // written slots
+    unsigned long long* n_done;     // completed items
     double* rh;                     // [n_ts + 1][n_reach_int] reach outflow per step
     const int2* heads;              // (headwater reach, 0) items, ready at the start
     int n_heads;
+    int continue_items;             // 1: a lane continues with an item it made ready
     unsigned long long n_items;     // real reaches x n_ts
 };
 

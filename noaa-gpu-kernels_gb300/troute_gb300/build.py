@@ -64,6 +64,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     # No implicit FMA contraction: the solver then rounds every +, -, *, / like
     # the reference's C on the host (explicit fma() calls are unaffected).
     fmad = ["-fmad=false"] if os.environ.get("TROUTE_FMAD", "0") == "0" else []
+    # TROUTE_CHECK=1: self-checking kernels (dependency and bounds invariants are
+    # verified on the device and reported as errors instead of being assumed)
+    if os.environ.get("TROUTE_CHECK", "0") == "1":
+        fmad = fmad + ["-DTROUTE_CHECK"]
+    fmad = fmad + [f"-D{d}" for d in os.environ.get("TROUTE_DEFINES", "").split() if d]
     for f in CU_SOURCES:
         o = os.path.join(BUILD, f + ".o")
         objs.append(o)
