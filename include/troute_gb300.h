@@ -130,6 +130,23 @@ int troute_mc_reach_parallel_device(const troute_chparams* p, const double* ql,
                                     double uq, double dt, int nr, int n_segments,
                                     const troute_cfg* cfg, void* stream);
 
+/* Same computation as troute_mc_reach_parallel_device for callers that cannot
+ * allocate device memory (stream capture in progress, device memory owned by
+ * another framework or pool): its only scratch, the per-block solve counters,
+ * is an array compiled into the library (about 1.7 MB per GPU, held until the
+ * process exits). No counterpart in the reference. At most 2,097,152 reaches per
+ * call (larger calls return TROUTE_EINVAL). The first call on a device looks up
+ * the array's address with that device current: make it before any stream
+ * capture. Calls that overlap on the GPU share the array and race. With stats
+ * non-NULL the call waits for `stream` and returns the counters. */
+int troute_mc_reach_parallel_device_noalloc(const troute_chparams* p, const double* ql,
+                                            const int* rs, const int* rl,
+                                            const double* qu, const double* qd, const double* dp,
+                                            double* qo, double* vo, double* dpo,
+                                            double uq, double dt, int nr, int n_segments,
+                                            const troute_cfg* cfg, void* stream,
+                                            troute_stats* stats);
+
 /* ---- level-scheduled tree routing, multi-step (replaces
  *      cpu_wavefront_fp64, wavefront_mc.cu:495-507) ----------------------- */
 /* Exact argument list of cpu_wavefront_fp64 (float inputs, double outputs,
