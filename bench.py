@@ -332,7 +332,7 @@ def run_ours(args, dist: Dist):
                        "l2": "inputs larger than L2 (lateral inflow 3.1 GB read per step)",
                        "parallelism": "replicas" if dist.world > 1 else "single GPU"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": 4 * args.steps,
             "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
                        "early_exits": stats["early_exits"]}}
     if dist.rank == 0:
