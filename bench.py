@@ -171,9 +171,56 @@ def profiled_traffic_per_seg_step():
 
 
 def workload(name: str, n_ts: int | None):
+    """Single networks ('c1', 'c0', 'tree:<segments>') or the batched forms:
+    'c2' (256 basins with LogU(500, 200,000) segments, 288 steps) and
+    'c4' (64 ensemble members of the c1 network, 288 steps)."""
     from troute_gb300 import synth
 
-    return synth.network(name, n_ts=n_ts)
+    if name == "c2":
+        nets = synth.basins(seed=1002, n_trees=256)
+        T = 288 if n_ts is None else n_ts
+        S = sum(n["topo"]["n_segments"] for n in nets)
+        w = {"name": name, "batch": nets, "n_ts": T, "dt": synth.DT,
+             "qlat": synth.make_qlat(1002, S, T)}
+        w["q0"] = np.full(S, synth.Q0)
+        w["d0"] = np.full(S, synth.D0)
+        w["rl0"] = np.concatenate([np.full(len(n["topo"]["reach_seg_start"]), synth.Q0) for n in nets])
+        w["S"], w["R"] = S, len(w["rl0"])
+        return w
+    if name == "c4":
+        M = 64
+        T = 288 if n_ts is None else n_ts
+        w = synth.network("c1", n_ts=T)
+        S = w["topo"]["n_segments"]
+        qf = np.empty((M, S))
+        nf = np.empty((M, S))
+        for m in range(M):
+            qf[m], nf[m] = synth.make_member(1004, m, S)
+        w.update(name=name, members=M, qfac=qf, nfac=nf)
+        w["S"], w["R"] = M * S, M * len(w["topo"]["reach_seg_start"])
+        w["q0"], w["d0"], w["rl0"] = np.tile(w["q0"], M), np.tile(w["d0"], M), np.tile(w["rl0"], M)
+        return w
+    w = synth.network(name, n_ts=n_ts)
+    w["S"], w["R"] = w["topo"]["n_segments"], len(w["topo"]["reach_seg_start"])
+    return w
+
+
+def make_network(T, w, cfg):
+    if "batch" in w:
+        nets = w["batch"]
+        return T.Network([n["topo"] for n in nets], [n["params"] for n in nets], cfg=cfg)
+    if "members" in w:
+        return T.Network.ensemble(w["topo"], w["params"], w["members"], n_scale=w["nfac"], qlat_scale=w["qfac"],
+                                  cfg=cfg)
+    return T.Network(w["topo"], w["params"], cfg=cfg)
+
+
+def describe(w) -> str:
+    if "batch" in w:
+        return f"batched: {len(w['batch'])} independent basins in one launch"
+    if "members" in w:
+        return f"batched: {w['members']}-member ensemble in one launch"
+    return "plain, single basin"
 
 
 def cpu_baseline(w) -> dict:
@@ -241,16 +288,17 @@ def run_ours(args, dist: Dist):
     dev = torch.device("cuda", dist.local if dist.world > 1 else 0)
     torch.cuda.set_device(dev)
     w = workload(args.workload, args.n_ts)
-    topo = w["topo"]
-    S, R = topo["n_segments"], len(topo["reach_seg_start"])
+    S, R = w["S"], w["R"]
     n_ts = w["qlat"].shape[0]
+    cols = w["qlat"].shape[1]
     cfg = T.make_cfg(**TIGHT)
-    net = T.Network(topo, w["params"], cfg=cfg)
+    net = make_network(T, w, cfg)
     net.set_state(w["q0"], w["d0"], w["rl0"])
-    qlat_host = torch.empty((n_ts, S), dtype=torch.float64, pin_memory=True)
+    qlat_host = torch.empty((n_ts, cols), dtype=torch.float64, pin_memory=True)
     qlat_host.numpy()[:] = w["qlat"]
     qlat_dev = qlat_host.to(dev, non_blocking=False)
     stream = torch.cuda.Stream(dev)   # a real stream: 0 would mean "the handle's own stream"
+    levels = net.n_levels
     net.graph_capture(qlat_dev.data_ptr(), n_ts)
     for _ in range(args.warmup):
         net.graph_launch(stream.cuda_stream)
@@ -300,7 +348,8 @@ def run_ours(args, dist: Dist):
         # public C-ABI path with host buffers: H2D of the step's lateral inflow
         # from pinned memory inside troute_run, D2H of the routed state
         qh = qlat_host.numpy()
-        net2 = T.Network(topo, w["params"], cfg=cfg)
+        net.close()
+        net2 = make_network(T, w, cfg)
         net2.set_state(w["q0"], w["d0"], w["rl0"])
         for _ in range(1):
             net2.run(qh)
@@ -319,16 +368,16 @@ def run_ours(args, dist: Dist):
         net2.close()
 
     cpu = None
-    if dist.rank == 0 and not args.no_cpu_baseline:
+    if dist.rank == 0 and not args.no_cpu_baseline and "topo" in w and "members" not in w:
         cpu = cpu_baseline(w)
     it = stats["iterations"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-            "config": {"workload": f"{args.workload}: FP64 MC secant tree routing (plain, single basin), "
-                                   f"{S} segments, {R} reaches, {net.n_levels} levels, {n_ts} steps of "
+            "config": {"workload": f"{args.workload}: FP64 MC secant tree routing ({describe(w)}), "
+                                   f"{S} segments, {R} reaches, {levels} levels, {n_ts} steps of "
                                    f"{w['dt']:.0f} s per bench step, rtol 1e-8 atol 1e-10",
-                       "segments": S, "reaches": R, "levels": net.n_levels, "timesteps_per_step": n_ts,
+                       "segments": S, "reaches": R, "levels": levels, "timesteps_per_step": n_ts,
                        "l2": "inputs larger than L2 (lateral inflow 3.1 GB read per step)",
                        "parallelism": "replicas" if dist.world > 1 else "single GPU"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
@@ -337,7 +386,6 @@ def run_ours(args, dist: Dist):
                        "early_exits": stats["early_exits"]}}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
-    net.close()
 
 
 def main():

@@ -63,7 +63,9 @@ typedef struct troute_cfg {
     int mapping;            /* reach-to-warp mapping: 0 auto (3), 1 one level-block per
                                warp, 2 per-lane refill in level-block order,
                                3 per-lane refill from the ready queue */
-    int reserved[6];
+    int schedule_flags;     /* mapping 3, bit 0: a lane continues with an item it made ready */
+    int max_chunk_steps;    /* steps routed per launch (0: as many as a third of free memory allows) */
+    int reserved[4];
 } troute_cfg;
 
 /* Counters of one run (summed over all segment solves). */
@@ -184,6 +186,15 @@ int troute_create_batch(troute_handle** h, int n_nets, const troute_topo* topos,
                         const troute_chparams* const* params,
                         const int* const* qlat_col, const double* const* qlat_scale,
                         int qlat_cols, double dt, const troute_cfg* cfg);
+/* Ensemble form: n_members copies of one network in one launch; member m
+ * routes the network with Manning's n (channel and floodplain) times
+ * n_scale[m][s] and lateral inflow column s times qlat_scale[m][s] (either
+ * scale may be NULL = 1). Lateral inflow is one base [n_ts][n_segments]
+ * matrix shared by all members; state is member-major. */
+int troute_create_ensemble(troute_handle** h, const troute_topo* topo,
+                           const troute_chparams* params, int n_members,
+                           const double* n_scale, const double* qlat_scale,
+                           double dt, const troute_cfg* cfg);
 int troute_destroy(troute_handle* h);
 int troute_set_cfg(troute_handle* h, const troute_cfg* cfg);
 /* Network sizes (any pointer may be NULL). */

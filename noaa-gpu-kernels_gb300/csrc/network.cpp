@@ -179,7 +179,9 @@ struct troute_handle {
     DBuf<int> qcol, nseg, block_level, lb_ptr_d, up_ptr, up_idx, down, done, step_base;
     DBuf<double> qscale, q, d, v, ring, tmp, qlat_buf, hist;
     DBuf<long long> tile_off, seg_map_d, reach_map_d;
-    DBuf<unsigned long long> wave_ptr, ticket, rq_ctr;
+    DBuf<unsigned long long> wave_ptr, wave_ptr_tail, ticket, rq_ctr;
+    unsigned long long n_tickets = 0, n_tickets_tail = 0;
+    size_t chunk_budget_bytes = 0;
     DBuf<int> df_cnt;
     DBuf<int2> df_rq, df_heads;
     DBuf<double> df_rh;
@@ -230,7 +232,7 @@ struct troute_handle {
         up_ptr.release(); up_idx.release(); down.release(); done.release(); step_base.release();
         qscale.release(); q.release(); d.release(); v.release(); ring.release(); tmp.release();
         qlat_buf.release(); hist.release(); tile_off.release(); seg_map_d.release();
-        reach_map_d.release(); wave_ptr.release(); ticket.release(); stats.release();
+        reach_map_d.release(); wave_ptr.release(); wave_ptr_tail.release(); ticket.release(); stats.release();
         rq_ctr.release(); df_cnt.release(); df_rq.release(); df_heads.release(); df_rh.release();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -271,19 +273,43 @@ static int launch_shape(troute_handle* H)
     return TROUTE_OK;
 }
 
-// Builds the device schedule for a forest and uploads everything.
-static int build_handle(troute_handle* H, const Forest& f, const std::vector<troute_chparams>& params,
+// Host image of everything a handle uploads (internal order).
+struct Layout {
+    int R_user = 0, S_user = 0, n_levels = 0, NB = 0, R_int = 0, n_heads = 0, R_real = 0;
+    long long S_int = 0;  // tiles + 1 trash slot
+    std::vector<int> user_seg_start, user_seg_len;
+    std::vector<int> lb_ptr, block_level, nseg, up_ptr, up_idx, down_i, qcol;
+    std::vector<long long> tile_off, seg_map, reach_map;  // seg_map: -1 for uncovered segments
+    std::vector<int2> heads;
+    std::vector<double2> planes[kParamPlanes];
+    std::vector<double> qscale;  // empty: no scaling
+};
+
+static void put_params(Layout& Lt, long long t, const troute_chparams& c)
+{
+    const SegP p = derive_seg(c);
+    Lt.planes[0][t] = double2{p.dx, p.bw};
+    Lt.planes[1][t] = double2{p.twcc, p.n_ch};
+    Lt.planes[2][t] = double2{p.ncc, p.s0};
+    Lt.planes[3][t] = double2{p.z, p.bfd};
+    Lt.planes[4][t] = double2{p.sq_s0, p.sq_1z2};
+    Lt.planes[5][t] = double2{p.ck_fac, p.inv_n};
+}
+
+// Schedule and layout of a forest (ALAP levels, level-blocks, tiles).
+static int build_layout(const Forest& f, const std::vector<troute_chparams>& params,
                         const std::vector<int>& qcol_user, const std::vector<double>& qscale_user,
-                        bool has_scale)
+                        bool has_scale, Layout& Lt)
 {
     std::vector<int> down, order;
     int rc = validate_forest(f, down, order);
     if (rc) return rc;
     const int R = f.R;
-    H->R_user = R;
-    H->S_user = f.S;
-    H->user_seg_start = f.seg_start;
-    H->user_seg_len = f.seg_len;
+    Lt.R_user = R;
+    Lt.S_user = f.S;
+    Lt.R_real = R;
+    Lt.user_seg_start = f.seg_start;
+    Lt.user_seg_len = f.seg_len;
 
     // ALAP level: distance to the outlet, counted down from the deepest level.
     std::vector<int> dist(R, 0);
@@ -294,113 +320,216 @@ static int build_handle(troute_handle* H, const Forest& f, const std::vector<tro
         maxd = std::max(maxd, dist[r]);
     }
     const int L = (R > 0) ? maxd + 1 : 0;
-    H->n_levels = L;
+    Lt.n_levels = L;
     std::vector<std::vector<int>> by_level(L);
     for (int r = 0; r < R; ++r) by_level[L - 1 - dist[r]].push_back(r);
-    std::vector<int> lb_ptr(L + 1, 0), block_level;
+    Lt.lb_ptr.assign(L + 1, 0);
     std::vector<std::vector<int>> blocks;
     for (int l = 0; l < L; ++l) {
         auto& v = by_level[l];
         std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return f.seg_len[a] > f.seg_len[b]; });
         for (size_t i = 0; i < v.size(); i += kLanes) {
             blocks.emplace_back(v.begin() + i, v.begin() + std::min(v.size(), i + kLanes));
-            block_level.push_back(l);
+            Lt.block_level.push_back(l);
         }
-        lb_ptr[l + 1] = (int)blocks.size();
+        Lt.lb_ptr[l + 1] = (int)blocks.size();
     }
     const int NB = (int)blocks.size();
-    H->n_blocks = NB;
-    H->R_int = NB * kLanes;
-    H->lb_ptr = lb_ptr;
+    Lt.NB = NB;
+    Lt.R_int = NB * kLanes;
 
-    std::vector<long long> tile_off(NB);
+    Lt.tile_off.assign(NB, 0);
     long long S_int = 0;
-    H->reach_map.assign(R, -1);
-    H->seg_map.assign(f.S, -1);
-    std::vector<int> nseg(H->R_int, -1);
+    Lt.reach_map.assign(R, -1);
+    Lt.seg_map.assign(f.S, -1);
+    Lt.nseg.assign(Lt.R_int, -1);
     for (int b = 0; b < NB; ++b) {
-        tile_off[b] = S_int;
+        Lt.tile_off[b] = S_int;
         int hmax = 0;
         for (size_t k = 0; k < blocks[b].size(); ++k) {
             const int r = blocks[b][k];
             const int ri = b * kLanes + (int)k;
-            H->reach_map[r] = ri;
-            nseg[ri] = f.seg_len[r];
+            Lt.reach_map[r] = ri;
+            Lt.nseg[ri] = f.seg_len[r];
             hmax = std::max(hmax, f.seg_len[r]);
             for (int i = 0; i < f.seg_len[r]; ++i)
-                H->seg_map[f.seg_start[r] + i] = S_int + (long long)i * kLanes + (long long)k;
+                Lt.seg_map[f.seg_start[r] + i] = S_int + (long long)i * kLanes + (long long)k;
         }
         S_int += (long long)hmax * kLanes;
     }
     // one extra slot at the end: the target of segments no reach covers, so
     // scatter/gather through the segment map never leave the planes
-    const long long trash = S_int;
-    H->S_int = S_int + 1;
-    std::vector<long long> seg_map_dev(H->seg_map);
-    for (auto& m : seg_map_dev)
-        if (m < 0) m = trash;
+    Lt.S_int = S_int + 1;
 
     // upstream CSR over internal ids, keeping each reach's upstream order
     // (the order of the floating-point sum at the reach head)
-    std::vector<int> up_ptr(H->R_int + 1, 0), up_idx, down_i(H->R_int, -1);
-    up_idx.reserve(f.up_idx.size());
+    Lt.up_ptr.assign(Lt.R_int + 1, 0);
+    Lt.down_i.assign(Lt.R_int, -1);
+    Lt.up_idx.reserve(f.up_idx.size());
     {
-        std::vector<int> user_of(H->R_int, -1);
-        for (int r = 0; r < R; ++r) user_of[H->reach_map[r]] = r;
-        for (int ri = 0; ri < H->R_int; ++ri) {
+        std::vector<int> user_of(Lt.R_int, -1);
+        for (int r = 0; r < R; ++r) user_of[Lt.reach_map[r]] = r;
+        for (int ri = 0; ri < Lt.R_int; ++ri) {
             const int r = user_of[ri];
             if (r >= 0) {
                 for (int k = f.up_ptr[r]; k < f.up_ptr[r + 1]; ++k)
-                    up_idx.push_back((int)H->reach_map[f.up_idx[k]]);
-                if (down[r] >= 0) down_i[ri] = (int)H->reach_map[down[r]];
+                    Lt.up_idx.push_back((int)Lt.reach_map[f.up_idx[k]]);
+                if (down[r] >= 0) Lt.down_i[ri] = (int)Lt.reach_map[down[r]];
             }
-            up_ptr[ri + 1] = (int)up_idx.size();
+            Lt.up_ptr[ri + 1] = (int)Lt.up_idx.size();
         }
     }
-
     // items ready at the start of a run: reaches without upstream reaches, step 0
-    {
-        std::vector<int2> heads;
-        for (int ri = 0; ri < H->R_int; ++ri)
-            if (nseg[ri] >= 0 && up_ptr[ri + 1] == up_ptr[ri]) heads.push_back(int2{ri, 0});
-        H->n_heads = (int)heads.size();
-        H->R_real = R;
-        if ((rc = upload(H->df_heads, heads.empty() ? std::vector<int2>{int2{0, 0}} : heads, H->stream))) return rc;
-    }
+    for (int ri = 0; ri < Lt.R_int; ++ri)
+        if (Lt.nseg[ri] >= 0 && Lt.up_ptr[ri + 1] == Lt.up_ptr[ri]) Lt.heads.push_back(int2{ri, 0});
+    Lt.n_heads = (int)Lt.heads.size();
 
     // parameters in tile order
-    std::vector<double2> planes[kParamPlanes];
-    for (auto& p : planes) p.assign(H->S_int, double2{0.0, 0.0});
-    std::vector<int> qcol(H->S_int, 0);
-    std::vector<double> qscale(has_scale ? H->S_int : 0, 0.0);
+    for (auto& p : Lt.planes) p.assign(Lt.S_int, double2{0.0, 0.0});
+    Lt.qcol.assign(Lt.S_int, 0);
+    if (has_scale) Lt.qscale.assign(Lt.S_int, 0.0);
     for (int s = 0; s < f.S; ++s) {
-        const long long t = H->seg_map[s];
+        const long long t = Lt.seg_map[s];
         if (t < 0) continue;
-        const SegP p = derive_seg(params[s]);
-        planes[0][t] = double2{p.dx, p.bw};
-        planes[1][t] = double2{p.twcc, p.n_ch};
-        planes[2][t] = double2{p.ncc, p.s0};
-        planes[3][t] = double2{p.z, p.bfd};
-        planes[4][t] = double2{p.sq_s0, p.sq_1z2};
-        planes[5][t] = double2{p.ck_fac, p.inv_n};
-        qcol[t] = qcol_user[s];
-        if (has_scale) qscale[t] = qscale_user[s];
+        put_params(Lt, t, params[s]);
+        Lt.qcol[t] = qcol_user[s];
+        if (has_scale) Lt.qscale[t] = qscale_user[s];
     }
+    return TROUTE_OK;
+}
+
+// Layout of M copies of one network (ensemble members): same topology and
+// schedule, member m's Manning's n (channel and floodplain) scaled by
+// n_scale[m][s] and its lateral inflow by q_scale[m][s] (NULL: 1). Blocks are
+// ordered level by level (members of one level together), tiles member-major.
+static void replicate_layout(const Layout& B, const std::vector<troute_chparams>& params, int M,
+                             const double* n_scale, const double* q_scale, Layout& E)
+{
+    const long long tiles = B.S_int - 1;
+    const int S = B.S_user, R = B.R_user, L = B.n_levels;
+    E.R_user = R * M;
+    E.S_user = S * M;
+    E.R_real = B.R_real * M;
+    E.n_levels = L;
+    E.NB = B.NB * M;
+    E.R_int = E.NB * kLanes;
+    E.S_int = tiles * M + 1;
+    E.user_seg_start.resize((size_t)E.R_user);
+    E.user_seg_len.resize((size_t)E.R_user);
+    for (int m = 0; m < M; ++m)
+        for (int r = 0; r < R; ++r) {
+            E.user_seg_start[(size_t)m * R + r] = B.user_seg_start[r] + m * S;
+            E.user_seg_len[(size_t)m * R + r] = B.user_seg_len[r];
+        }
+    // block b of level l, member m -> M*lb_ptr[l] + m*nb_l + (b - lb_ptr[l])
+    std::vector<int> new_block((size_t)B.NB * M);
+    E.lb_ptr.assign(L + 1, 0);
+    E.block_level.resize((size_t)E.NB);
+    for (int l = 0; l < L; ++l) {
+        const int b0 = B.lb_ptr[l], nb = B.lb_ptr[l + 1] - b0;
+        E.lb_ptr[l + 1] = M * B.lb_ptr[l + 1];
+        for (int m = 0; m < M; ++m)
+            for (int j = 0; j < nb; ++j) {
+                const int nbk = M * b0 + m * nb + j;
+                new_block[(size_t)m * B.NB + b0 + j] = nbk;
+                E.block_level[nbk] = l;
+            }
+    }
+    auto new_reach = [&](int m, int ri) { return new_block[(size_t)m * B.NB + ri / kLanes] * kLanes + ri % kLanes; };
+    E.tile_off.assign((size_t)E.NB, 0);
+    E.nseg.assign((size_t)E.R_int, -1);
+    E.down_i.assign((size_t)E.R_int, -1);
+    std::vector<int> up_cnt((size_t)E.R_int, 0);
+    for (int m = 0; m < M; ++m)
+        for (int b = 0; b < B.NB; ++b) {
+            E.tile_off[new_block[(size_t)m * B.NB + b]] = B.tile_off[b] + (long long)m * tiles;
+            for (int k = 0; k < kLanes; ++k) {
+                const int ri = b * kLanes + k, ni = new_reach(m, ri);
+                E.nseg[ni] = B.nseg[ri];
+                E.down_i[ni] = B.down_i[ri] >= 0 ? new_reach(m, B.down_i[ri]) : -1;
+                up_cnt[ni] = B.up_ptr[ri + 1] - B.up_ptr[ri];
+            }
+        }
+    E.up_ptr.assign((size_t)E.R_int + 1, 0);
+    for (int ri = 0; ri < E.R_int; ++ri) E.up_ptr[ri + 1] = E.up_ptr[ri] + up_cnt[ri];
+    E.up_idx.assign((size_t)E.up_ptr[E.R_int], 0);
+    for (int m = 0; m < M; ++m)
+        for (int ri = 0; ri < B.R_int; ++ri) {
+            const int ni = new_reach(m, ri);
+            for (int k = B.up_ptr[ri]; k < B.up_ptr[ri + 1]; ++k)
+                E.up_idx[E.up_ptr[ni] + (k - B.up_ptr[ri])] = new_reach(m, B.up_idx[k]);
+        }
+    for (int m = 0; m < M; ++m)
+        for (const int2& h : B.heads) E.heads.push_back(int2{new_reach(m, h.x), 0});
+    E.n_heads = (int)E.heads.size();
+    E.reach_map.resize((size_t)E.R_user);
+    E.seg_map.resize((size_t)E.S_user);
+    for (int m = 0; m < M; ++m) {
+        for (int r = 0; r < R; ++r) E.reach_map[(size_t)m * R + r] = new_reach(m, (int)B.reach_map[r]);
+        for (int s = 0; s < S; ++s)
+            E.seg_map[(size_t)m * S + s] = B.seg_map[s] < 0 ? -1 : B.seg_map[s] + (long long)m * tiles;
+    }
+    for (auto& p : E.planes) p.assign((size_t)E.S_int, double2{0.0, 0.0});
+    E.qcol.assign((size_t)E.S_int, 0);
+    E.qscale.assign(q_scale ? (size_t)E.S_int : 0, 0.0);
+    for (int m = 0; m < M; ++m)
+        for (int s = 0; s < S; ++s) {
+            const long long bt = B.seg_map[s];
+            if (bt < 0) continue;
+            const long long t = bt + (long long)m * tiles;
+            troute_chparams c = params[s];
+            if (n_scale) {
+                const double f = n_scale[(size_t)m * S + s];
+                c.n_ch *= f;
+                c.ncc *= f;
+            }
+            put_params(E, t, c);
+            E.qcol[t] = B.qcol[bt];
+            if (q_scale) E.qscale[t] = q_scale[(size_t)m * S + s];
+        }
+}
+
+// Uploads a layout into a handle and allocates its state.
+static int upload_layout(troute_handle* H, Layout& Lt)
+{
+    int rc;
+    H->R_user = Lt.R_user;
+    H->S_user = Lt.S_user;
+    H->R_real = Lt.R_real;
+    H->user_seg_start = std::move(Lt.user_seg_start);
+    H->user_seg_len = std::move(Lt.user_seg_len);
+    H->n_levels = Lt.n_levels;
+    H->n_blocks = Lt.NB;
+    H->R_int = Lt.R_int;
+    H->S_int = Lt.S_int;
+    H->lb_ptr = Lt.lb_ptr;
+    H->n_heads = Lt.n_heads;
+    H->seg_map = Lt.seg_map;
+    H->reach_map = Lt.reach_map;
+    const long long trash = Lt.S_int - 1;
+    std::vector<long long> seg_map_dev(std::move(Lt.seg_map));
+    for (auto& m : seg_map_dev)
+        if (m < 0) m = trash;
 
     cudaStream_t st = H->stream;
-    for (int i = 0; i < kParamPlanes; ++i)
-        if ((rc = upload(H->prm[i], planes[i], st))) return rc;
-    if ((rc = upload(H->qcol, qcol, st))) return rc;
-    if (has_scale && (rc = upload(H->qscale, qscale, st))) return rc;
-    if ((rc = upload(H->nseg, nseg, st))) return rc;
-    if ((rc = upload(H->tile_off, tile_off, st))) return rc;
-    if ((rc = upload(H->block_level, block_level, st))) return rc;
-    if ((rc = upload(H->lb_ptr_d, lb_ptr, st))) return rc;
-    if ((rc = upload(H->up_ptr, up_ptr, st))) return rc;
-    if ((rc = upload(H->up_idx, up_idx.empty() ? std::vector<int>{0} : up_idx, st))) return rc;
-    if ((rc = upload(H->down, down_i, st))) return rc;
+    for (int i = 0; i < kParamPlanes; ++i) {
+        if ((rc = upload(H->prm[i], Lt.planes[i], st))) return rc;
+        if ((rc = cuda_check(cudaStreamSynchronize(st), "upload"))) return rc;
+        std::vector<double2>().swap(Lt.planes[i]);
+    }
+    if ((rc = upload(H->qcol, Lt.qcol, st))) return rc;
+    if (!Lt.qscale.empty() && (rc = upload(H->qscale, Lt.qscale, st))) return rc;
+    if ((rc = upload(H->nseg, Lt.nseg, st))) return rc;
+    if ((rc = upload(H->tile_off, Lt.tile_off, st))) return rc;
+    if ((rc = upload(H->block_level, Lt.block_level, st))) return rc;
+    if ((rc = upload(H->lb_ptr_d, Lt.lb_ptr, st))) return rc;
+    if ((rc = upload(H->up_ptr, Lt.up_ptr, st))) return rc;
+    if ((rc = upload(H->up_idx, Lt.up_idx.empty() ? std::vector<int>{0} : Lt.up_idx, st))) return rc;
+    if ((rc = upload(H->down, Lt.down_i, st))) return rc;
+    if ((rc = upload(H->df_heads, Lt.heads.empty() ? std::vector<int2>{int2{0, 0}} : Lt.heads, st))) return rc;
     if ((rc = upload(H->seg_map_d, seg_map_dev.empty() ? std::vector<long long>{trash} : seg_map_dev, st))) return rc;
     if ((rc = upload(H->reach_map_d, H->reach_map.empty() ? std::vector<long long>{0} : H->reach_map, st))) return rc;
+    if ((rc = cuda_check(cudaStreamSynchronize(st), "upload"))) return rc;
     if ((rc = H->q.alloc(H->S_int)) || (rc = H->d.alloc(H->S_int)) || (rc = H->v.alloc(H->S_int))) return rc;
     if ((rc = H->ring.alloc((size_t)kRing * std::max(1, H->R_int)))) return rc;
     if ((rc = H->done.alloc(std::max(1, H->R_int))) || (rc = H->step_base.alloc(1))) return rc;
@@ -412,9 +541,18 @@ static int build_handle(troute_handle* H, const Forest& f, const std::vector<tro
     if ((rc = cuda_check(cudaMemsetAsync(H->ring.p, 0, H->ring.n * sizeof(double), st), "memset"))) return rc;
     if ((rc = cuda_check(cudaMemsetAsync(H->done.p, 0, H->done.n * sizeof(int), st), "memset"))) return rc;
     if ((rc = cuda_check(cudaMemsetAsync(H->step_base.p, 0, sizeof(int), st), "memset"))) return rc;
-
     if ((rc = launch_shape(H))) return rc;
     return cuda_check(cudaStreamSynchronize(st), "build sync");
+}
+
+static int build_handle(troute_handle* H, const Forest& f, const std::vector<troute_chparams>& params,
+                        const std::vector<int>& qcol_user, const std::vector<double>& qscale_user,
+                        bool has_scale)
+{
+    Layout Lt;
+    int rc = build_layout(f, params, qcol_user, qscale_user, has_scale, Lt);
+    if (rc) return rc;
+    return upload_layout(H, Lt);
 }
 
 static int new_handle(troute_handle** out, double dt, const troute_cfg* cfg)
@@ -520,6 +658,36 @@ extern "C" int troute_create(troute_handle** h, const troute_topo* topo, const t
     if (!topo) return set_error(TROUTE_EINVAL, "null topology");
     const troute_chparams* p[1] = {params};
     return troute_create_batch(h, 1, topo, p, nullptr, nullptr, 0, dt, cfg);
+}
+
+extern "C" int troute_create_ensemble(troute_handle** h, const troute_topo* topo,
+                                      const troute_chparams* params, int n_members,
+                                      const double* n_scale, const double* qlat_scale,
+                                      double dt, const troute_cfg* cfg)
+{
+    if (!topo || n_members < 1) return set_error(TROUTE_EINVAL, "ensemble needs a topology and n_members >= 1");
+    if (topo->n_segments > 0 && !params) return set_error(TROUTE_EINVAL, "null params");
+    if ((long long)n_members * topo->n_segments > 0x7FFFFFFFLL || (long long)n_members * topo->n_reaches > 0x3FFFFFFFLL)
+        return set_error(TROUTE_EINVAL, "ensemble too large for 32-bit segment/reach indices");
+    Forest f;
+    f.up_ptr.push_back(0);
+    if (!append_topo(f, *topo)) return set_error(TROUTE_ETOPO, "malformed topology arrays");
+    std::vector<troute_chparams> prm(params, params + f.S);
+    std::vector<int> qc(f.S);
+    for (int s = 0; s < f.S; ++s) qc[s] = s;
+    Layout base, ens;
+    int rc = build_layout(f, prm, qc, std::vector<double>(), false, base);
+    if (rc) return rc;
+    replicate_layout(base, prm, n_members, n_scale, qlat_scale, ens);
+    troute_handle* H = nullptr;
+    if ((rc = new_handle(&H, dt, cfg))) return rc;
+    H->qlat_cols = f.S;
+    if ((rc = upload_layout(H, ens))) {
+        delete H;
+        return rc;
+    }
+    *h = H;
+    return TROUTE_OK;
 }
 
 extern "C" int troute_destroy(troute_handle* h)
@@ -636,8 +804,38 @@ static void wave_prefix(const std::vector<int>& lb_ptr, int L, int n_ts, std::ve
     }
 }
 
-// Enqueues one run (wave table already on the device) on stream `st`.
-static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, cudaStream_t st, bool timed)
+// A run of n_ts steps is routed in chunks whose per-step scratch (dependency
+// counters, ready-queue entries and outflow history of the dataflow kernel,
+// ~20 B per reach-step) fits a memory budget: cfg.max_chunk_steps if set,
+// else a third of the free device memory at the first run.
+struct RunPlan {
+    int chunk = 0, n_full = 0, rem = 0;
+};
+
+static int plan_run(troute_handle* H, int n_ts, RunPlan* P)
+{
+    int chunk = n_ts;
+    if (H->cfg.max_chunk_steps > 0) chunk = std::min(chunk, H->cfg.max_chunk_steps);
+    if (H->mapping == 3) {
+        const double per_step = (double)std::max(1, H->R_int) * (sizeof(int) + sizeof(double)) +
+                                (double)std::max(1, H->R_real) * sizeof(int2);
+        if (H->chunk_budget_bytes == 0) {
+            size_t fr = 0, tot = 0;
+            if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) fr = (size_t)8 << 30;
+            H->chunk_budget_bytes = fr / 3;
+        }
+        const long long fit = (long long)((double)H->chunk_budget_bytes / per_step);
+        chunk = (int)std::max<long long>(1, std::min<long long>(chunk, fit));
+    }
+    P->chunk = chunk;
+    P->n_full = n_ts / chunk;
+    P->rem = n_ts % chunk;
+    return TROUTE_OK;
+}
+
+// Enqueues one chunk of n_ts steps (wave table `wave` already on the device).
+static int enqueue_chunk(troute_handle* H, const double* qlat_dev, int n_ts, const unsigned long long* wave,
+                         unsigned long long n_tickets, double* q_hist, cudaStream_t st)
 {
     int rc;
     RunDev run;
@@ -646,19 +844,15 @@ static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, cudaS
     run.dt = H->dt;
     run.qlat = qlat_dev;
     run.qlat_ld = H->qlat_cols;
-    run.wave_ptr = H->wave_ptr.p;
+    run.wave_ptr = wave;
     run.n_waves = n_ts + H->n_levels - 1;
-    std::vector<unsigned long long> wp;
-    wave_prefix(H->lb_ptr, H->n_levels, n_ts, wp);
-    run.n_tickets = wp.back();
+    run.n_tickets = n_tickets;
     run.ticket = H->ticket.p;
     run.stats = H->stats.p;
     run.wait_cycles = H->cfg.wait_cycles > 0 ? H->cfg.wait_cycles : 8000000000LL;
     run.tol = make_tol(H->cfg);
-    run.q_hist = (H->cfg.record_history && H->hist.p) ? H->hist.p : nullptr;
+    run.q_hist = q_hist;
     if ((rc = cuda_check(cudaMemsetAsync(H->ticket.p, 0, sizeof(unsigned long long), st), "memset"))) return rc;
-    if ((rc = cuda_check(cudaMemsetAsync(H->stats.p, 0, sizeof(DevStats), st), "memset"))) return rc;
-    if (timed && (rc = cuda_check(cudaEventRecord(H->ev0, st), "event"))) return rc;
     if (H->mapping == 3) {
         DataflowDev df;
         df.cnt = H->df_cnt.p;
@@ -669,7 +863,7 @@ static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, cudaS
         df.rh = H->df_rh.p;
         df.heads = H->df_heads.p;
         df.n_heads = H->n_heads;
-        df.continue_items = H->cfg.reserved[0] & 1;
+        df.continue_items = H->cfg.schedule_flags & 1;
         df.n_items = (unsigned long long)H->R_real * (unsigned long long)n_ts;
         rc = launch_route_dataflow(H->net(), run, df, H->grid, st);
     } else if (H->mapping == 2) {
@@ -678,31 +872,65 @@ static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, cudaS
         rc = launch_route(H->net(), run, H->grid, H->threads, st);
     }
     if (rc) return rc;
-    if (H->mapping >= 2 && (rc = launch_velocity(H->net(), st))) return rc;
-    if (timed && (rc = cuda_check(cudaEventRecord(H->ev1, st), "event"))) return rc;
     return launch_bump_steps(H->step_base.p, n_ts, st);
 }
 
-static int prepare_run(troute_handle* H, int n_ts)
+// Enqueues a whole run as chunks; stats are zeroed once, the velocity of the
+// final state derived once at the end.
+static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, const RunPlan& P, cudaStream_t st,
+                       bool timed)
 {
     int rc;
+    if ((rc = cuda_check(cudaMemsetAsync(H->stats.p, 0, sizeof(DevStats), st), "memset"))) return rc;
+    if (timed && (rc = cuda_check(cudaEventRecord(H->ev0, st), "event"))) return rc;
+    const int n_chunks = P.n_full + (P.rem ? 1 : 0);
+    for (int c = 0; c < n_chunks; ++c) {
+        const int t0 = c * P.chunk;
+        const int len = (c < P.n_full) ? P.chunk : P.rem;
+        const bool tail = (c >= P.n_full);
+        const unsigned long long* wave = tail ? H->wave_ptr_tail.p : H->wave_ptr.p;
+        const unsigned long long nt = tail ? H->n_tickets_tail : H->n_tickets;
+        double* qh = (H->cfg.record_history && H->hist.p) ? H->hist.p + (size_t)t0 * H->S_int : nullptr;
+        if ((rc = enqueue_chunk(H, qlat_dev + (size_t)t0 * (size_t)H->qlat_cols, len, wave, nt, qh, st))) return rc;
+    }
+    if (H->mapping >= 2 && (rc = launch_velocity(H->net(), st))) return rc;
+    if (timed && (rc = cuda_check(cudaEventRecord(H->ev1, st), "event"))) return rc;
+    return TROUTE_OK;
+}
+
+static int upload_waves(troute_handle* H, int len, DBuf<unsigned long long>& buf, unsigned long long* n_tickets)
+{
     std::vector<unsigned long long> wp;
-    wave_prefix(H->lb_ptr, H->n_levels, n_ts, wp);
-    if ((rc = H->wave_ptr.alloc(wp.size()))) return rc;
-    if ((rc = cuda_check(cudaMemcpyAsync(H->wave_ptr.p, wp.data(), wp.size() * sizeof(unsigned long long),
-                                         cudaMemcpyHostToDevice, H->stream), "wave upload")))
-        return rc;
+    wave_prefix(H->lb_ptr, H->n_levels, len, wp);
+    *n_tickets = wp.back();
+    int rc = buf.alloc(wp.size());
+    if (rc) return rc;
+    rc = cuda_check(cudaMemcpyAsync(buf.p, wp.data(), wp.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                                    H->stream), "wave upload");
+    if (rc) return rc;
+    return cuda_check(cudaStreamSynchronize(H->stream), "wave sync");
+}
+
+static int prepare_run(troute_handle* H, int n_ts, RunPlan* P)
+{
+    int rc = plan_run(H, n_ts, P);
+    if (rc) return rc;
+    if (H->mapping != 3) {
+        if ((rc = upload_waves(H, P->chunk, H->wave_ptr, &H->n_tickets))) return rc;
+        if (P->rem && (rc = upload_waves(H, P->rem, H->wave_ptr_tail, &H->n_tickets_tail))) return rc;
+    }
     if (H->cfg.record_history) {
         if ((rc = H->hist.alloc((size_t)n_ts * H->S_int))) return rc;
         H->hist_ts = n_ts;
     }
     if (H->mapping == 3) {
         const size_t R = (size_t)std::max(1, H->R_int);
-        if ((rc = H->df_cnt.alloc((size_t)n_ts * R)) || (rc = H->df_rh.alloc((size_t)(n_ts + 1) * R)) ||
-            (rc = H->df_rq.alloc(std::max<size_t>(1, (size_t)H->R_real * (size_t)n_ts))) || (rc = H->rq_ctr.alloc(3)))
+        const size_t T = (size_t)P->chunk;
+        if ((rc = H->df_cnt.alloc(T * R)) || (rc = H->df_rh.alloc((T + 1) * R)) ||
+            (rc = H->df_rq.alloc(std::max<size_t>(1, (size_t)H->R_real * T))) || (rc = H->rq_ctr.alloc(3)))
             return rc;
     }
-    return cuda_check(cudaStreamSynchronize(H->stream), "wave sync");
+    return TROUTE_OK;
 }
 
 static int collect(troute_handle* H, troute_stats* stats, bool timed)
@@ -749,7 +977,8 @@ extern "C" int troute_run_device(troute_handle* h, const double* qlat_ts_device,
     if (n_ts < 0) return set_error(TROUTE_EINVAL, "n_ts < 0");
     if (n_ts == 0 || h->R_user == 0) return TROUTE_OK;
     if (!qlat_ts_device) return set_error(TROUTE_EINVAL, "null lateral inflow");
-    int rc = prepare_run(h, n_ts);
+    RunPlan P;
+    int rc = prepare_run(h, n_ts, &P);
     if (rc) return rc;
     cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
     if (stream) {
@@ -760,7 +989,7 @@ extern "C" int troute_run_device(troute_handle* h, const double* qlat_ts_device,
         cudaStreamWaitEvent(st, e, 0);
         cudaEventDestroy(e);
     }
-    if ((rc = enqueue_run(h, qlat_ts_device, n_ts, st, true))) return rc;
+    if ((rc = enqueue_run(h, qlat_ts_device, n_ts, P, st, true))) return rc;
     h->steps_done += n_ts;
     h->last_n_ts = n_ts;
     return TROUTE_OK;
@@ -797,12 +1026,13 @@ extern "C" int troute_run(troute_handle* h, const double* qlat_ts, int n_ts, tro
 extern "C" int troute_graph_capture(troute_handle* h, const double* qlat_ts_device, int n_ts)
 {
     if (!h || !qlat_ts_device || n_ts <= 0) return set_error(TROUTE_EINVAL, "bad graph arguments");
-    int rc = prepare_run(h, n_ts);
+    RunPlan P;
+    int rc = prepare_run(h, n_ts, &P);
     if (rc) return rc;
     if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
     if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
     if ((rc = cuda_check(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"))) return rc;
-    rc = enqueue_run(h, qlat_ts_device, n_ts, h->stream, false);
+    rc = enqueue_run(h, qlat_ts_device, n_ts, P, h->stream, false);
     cudaGraph_t g = nullptr;
     const int rc2 = cuda_check(cudaStreamEndCapture(h->stream, &g), "end capture");
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }

@@ -58,7 +58,9 @@ class Cfg(C.Structure):
         ("warm_k", C.c_int),
         ("record_history", C.c_int),
         ("mapping", C.c_int),
-        ("reserved", C.c_int * 6),
+        ("schedule_flags", C.c_int),
+        ("max_chunk_steps", C.c_int),
+        ("reserved", C.c_int * 4),
     ]
 
 
@@ -127,6 +129,7 @@ _SIGS = {
     "troute_route_tree": ([_P] * 6 + [_I, _D, _P] + [_P] * 5, _I),
     "troute_create": ([_P, _P, _P, _D, _P], _I),
     "troute_create_batch": ([_P, _I, _P, _P, _P, _P, _I, _D, _P], _I),
+    "troute_create_ensemble": ([_P, _P, _P, _I, _P, _P, _D, _P], _I),
     "troute_destroy": ([_P], _I),
     "troute_set_cfg": ([_P, _P], _I),
     "troute_info": ([_P, _P, _P, _P, _P, _P], _I),
@@ -306,7 +309,12 @@ class Network:
     """A routed network (or a batch of networks) with device-resident state."""
 
     def __init__(self, topos, params, dt: float = 300.0, cfg: Cfg | None = None, qlat_col=None, qlat_scale=None,
-                 qlat_cols: int = 0):
+                 qlat_cols: int = 0, _handle=None):
+        if _handle is not None:
+            self._h = _handle
+            self._keep = []
+            self._info()
+            return
         if isinstance(topos, dict):
             topos, params = [topos], [params]
             qlat_col = None if qlat_col is None else [qlat_col]
@@ -342,9 +350,29 @@ class Network:
                                          C.byref(cfg) if cfg is not None else None))
         self._h = h
         self._keep = []  # the library copied everything
+        self._info()
+
+    def _info(self):
         R, S, L, Q, T = _I(), _I(), _I(), _I(), C.c_longlong()
         _check(lib().troute_info(self._h, C.byref(R), C.byref(S), C.byref(L), C.byref(Q), C.byref(T)))
         self.n_reaches, self.n_segments, self.n_levels, self.qlat_cols = R.value, S.value, L.value, Q.value
+
+    @classmethod
+    def ensemble(cls, topo: dict, params, n_members: int, n_scale=None, qlat_scale=None, dt: float = 300.0,
+                 cfg: Cfg | None = None):
+        """n_members copies of one network (Manning's n and lateral inflow
+        scaled per member and segment); lateral inflow is the base
+        [n_ts][n_segments] matrix."""
+        ts, keep = _topo_struct(topo["reach_seg_start"], topo["reach_seg_len"], topo["reach_up_ptr"],
+                                topo["reach_up_idx"], topo["n_segments"])
+        pp = _params(params)
+        S = int(topo["n_segments"])
+        ns = None if n_scale is None else _f64(n_scale, n_members * S)
+        qs = None if qlat_scale is None else _f64(qlat_scale, n_members * S)
+        h = C.c_void_p()
+        _check(lib().troute_create_ensemble(C.byref(h), C.byref(ts), _ptr(pp), int(n_members), _ptr(ns), _ptr(qs),
+                                            float(dt), C.byref(cfg) if cfg is not None else None))
+        return cls(None, None, _handle=h)
 
     def close(self):
         if getattr(self, "_h", None):

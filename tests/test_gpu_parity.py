@@ -275,3 +275,60 @@ def test_tiny_wait_budget_reports_timeout_or_completes():
             net.set_state(c["q0"], c["d0"], c["rl0"])
             net.set_cfg(T.make_cfg())
             net.run(c["qlat"])
+
+
+def test_ensemble_members_bit_identical_to_single_runs():
+    c = synth.network("c0", n_ts=30)
+    S = c["topo"]["n_segments"]
+    M = 3
+    nf = np.stack([synth.make_member(21, m, S)[1] for m in range(M)])
+    qf = np.stack([synth.make_member(21, m, S)[0] for m in range(M)])
+    cfg = cfg_of(TIGHT)
+    with T.Network.ensemble(c["topo"], c["params"], M, n_scale=nf, qlat_scale=qf, cfg=cfg) as net:
+        assert net.n_segments == M * S and net.qlat_cols == S
+        net.set_state(np.tile(c["q0"], M), np.tile(c["d0"], M), np.tile(c["rl0"], M))
+        net.run(c["qlat"])
+        q, d, v, rl = net.get_state()
+    R = len(c["topo"]["reach_seg_start"])
+    for m in range(M):
+        p = c["params"].copy()
+        p["n_ch"] *= nf[m]
+        p["ncc"] *= nf[m]
+        with O.pow_mode(1):
+            o = O.route_tree(c["topo"], p, c["qlat"] * qf[m][None, :], c["q0"], c["d0"], c["rl0"], tol=TIGHT)
+        np.testing.assert_array_equal(q[m * S:(m + 1) * S], o["q"])
+        np.testing.assert_array_equal(d[m * S:(m + 1) * S], o["d"])
+        np.testing.assert_array_equal(v[m * S:(m + 1) * S], o["v"])
+        np.testing.assert_array_equal(rl[m * R:(m + 1) * R], o["reach_last"])
+
+
+@pytest.mark.parametrize("mapping", [3, 2, 1])
+def test_chunked_run_equals_single_launch(mapping):
+    c = synth.network("tree:5000", seed=12, n_ts=40)
+    args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    a = T.route_tree(*args, cfg=T.make_cfg(mapping=mapping), history=True)
+    b = T.route_tree(*args, cfg=T.make_cfg(mapping=mapping, max_chunk_steps=7), history=True)
+    for k in ("q", "d", "v", "reach_last", "q_hist"):
+        np.testing.assert_array_equal(a[k], b[k])
+    assert a["stats"]["iterations"] == b["stats"]["iterations"]
+
+
+def test_graph_replay_equals_runs():
+    torch = pytest.importorskip("torch")
+    c = synth.network("tree:5000", seed=13, n_ts=10)
+    ql = torch.from_numpy(np.ascontiguousarray(c["qlat"])).cuda()
+    with T.Network(c["topo"], c["params"], cfg=T.make_cfg(max_chunk_steps=4)) as g:
+        g.set_state(c["q0"], c["d0"], c["rl0"])
+        g.graph_capture(ql.data_ptr(), 10)
+        g.graph_launch()
+        g.graph_launch()
+        g.sync()
+        assert g.steps_done == 20
+        qg = g.get_state()
+    with T.Network(c["topo"], c["params"]) as r:
+        r.set_state(c["q0"], c["d0"], c["rl0"])
+        r.run(c["qlat"])
+        r.run(c["qlat"])
+        qr = r.get_state()
+    for x, y in zip(qg, qr):
+        np.testing.assert_array_equal(x, y)
