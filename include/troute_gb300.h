@@ -57,15 +57,18 @@ typedef struct troute_cfg {
     int threads_per_block;  /* 0: autotuned / default */
     int blocks_per_sm;      /* 0: occupancy-derived */
     long long wait_cycles;  /* bound on each device-side wait without progress, SM clocks; 0: ~4 s */
-    int warm_start;         /* 1: learned warm start (needs troute_set_warm_start) */
-    int warm_k;             /* iterations a warm-started solve gets before the plain solve */
+    int warm_start;         /* 1: learned warm start (needs troute_set_warm_start; mapping 3) */
+    int warm_k;             /* secant passes a warm-started solve gets before the plain solve */
     int record_history;     /* 1: keep per-step discharge of every segment (troute_get_history) */
     int mapping;            /* reach-to-warp mapping: 0 auto (3), 1 one level-block per
                                warp, 2 per-lane refill in level-block order,
                                3 per-lane refill from the ready queue */
     int schedule_flags;     /* mapping 3, bit 0: a lane continues with an item it made ready */
     int max_chunk_steps;    /* steps routed per launch (0: as many as a third of free memory allows) */
-    int reserved[4];
+    int record_pairs;       /* 1: every solve of a run keeps its training pair (troute_get_pairs) */
+    int record_start;       /* 1: every solve of a run keeps its learned starting depth
+                               (troute_get_start_history; 0 where the plain start was used) */
+    int reserved[2];
 } troute_cfg;
 
 /* Counters of one run (summed over all segment solves). */
@@ -224,6 +227,53 @@ int troute_get_history(troute_handle* h, double* q_hist, int n_ts);
  * count). nbytes: in = capacity, out = size; buf NULL queries the size. */
 int troute_checkpoint(troute_handle* h, void* buf, size_t* nbytes);
 int troute_restore(troute_handle* h, const void* buf, size_t nbytes);
+
+/* ---- learned warm start ------------------------------------------------ */
+/* No counterpart in the reference: its solve always starts from the previous
+ * depth (troute_mc_final.cu:193). An 8 -> 64 -> 64 -> 1 SiLU MLP predicts a
+ * segment's converged depth from log-standardised (qup, quc, qdp, ql, dx, s0,
+ * n, bw); trained on the device by the library's own forward / backward /
+ * AdamW kernels (FP32), evaluated inside the routing kernel with BF16 tensor
+ * cores (FP32 accumulate). A solve with a prediction p brackets
+ * [p (1 - delta), p (1 + delta)] for at most cfg.warm_k secant passes, then
+ * falls back to the plain solve from the previous depth. */
+typedef struct troute_warm troute_warm;
+/* Flat model state for get/set: W1 [64][8], b1 [64], W2 [64][64], b2 [64],
+ * w3 [64], b3, then the standardisation mu[8], sd[8], mu_y, sd_y. */
+#define TROUTE_WARM_NPARAMS 4801
+#define TROUTE_WARM_NSTATE (TROUTE_WARM_NPARAMS + 18)
+/* Training pair layout (floats): qup quc qdp ql dx s0 n bw depth. */
+#define TROUTE_PAIR_FLOATS 9
+
+int troute_warm_create(troute_warm** model, uint64_t seed);
+int troute_warm_destroy(troute_warm* model);
+int troute_warm_get(const troute_warm* model, float* state, int n);
+int troute_warm_set(troute_warm* model, const float* state, int n);
+/* Trains on n_pairs device-resident pairs: standardisation from the pairs,
+ * then `epochs` passes of shuffled mini-batches (batch a multiple of 64),
+ * AdamW (beta 0.9 / 0.999, decoupled weight decay) with a cosine-decayed step
+ * size from lr. loss_per_epoch (optional, [epochs]): mean of (err^2)/2 in
+ * standardised log-depth units. Synchronous. */
+int troute_warm_fit(troute_warm* model, const float* pairs_device, long long n_pairs, int epochs, int batch,
+                    float lr, float weight_decay, uint64_t seed, float* loss_per_epoch);
+/* Gradient of the loss over n host pairs at the current weights and
+ * standardisation (the training kernel's forward and backward pass):
+ * grad_out [TROUTE_WARM_NPARAMS], loss_out = mean (err^2)/2. */
+int troute_warm_grad(troute_warm* model, const float* pairs_host, int n, float* grad_out, double* loss_out);
+/* Predicted depths for n host input rows [n][8] (the tensor-core path). */
+int troute_warm_predict(troute_warm* model, const float* inputs_host, int n, double* depth_out);
+
+/* Attaches a trained model to a handle (NULL detaches); runs with
+ * cfg.warm_start = 1 use it. The model must outlive the handle's runs; a
+ * captured graph keeps the model's standardisation and delta of capture time. */
+int troute_set_warm_start(troute_handle* h, const troute_warm* model, double delta);
+/* Copies the training pairs of the last run (cfg.record_pairs) into a device
+ * buffer of `capacity` pairs, ordered by step then segment; *n_pairs = pairs
+ * available (solves that exit early have none). */
+int troute_get_pairs(troute_handle* h, float* pairs_device, long long capacity, long long* n_pairs);
+/* Learned starting depth of every solve of the last run (cfg.record_start),
+ * host [n_ts][n_segments]; 0 where the plain start was used. */
+int troute_get_start_history(troute_handle* h, double* start_hist, int n_ts);
 
 /* Launches a one-warp kernel whose wait on a flag nothing sets is bounded by
  * wait_cycles; returns TROUTE_ETIMEOUT once the wait gives up and the context

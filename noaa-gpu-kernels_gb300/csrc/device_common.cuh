@@ -36,7 +36,7 @@ __device__ inline void record_error(DevStats* st, int code, int reach, int step,
 
 // Per-thread counters, folded into the block's shared copy at the end.
 struct LocalStats {
-    unsigned long long solves, iterations, retries, early;
+    unsigned long long solves, iterations, retries, early, warm_used, warm_fallback;
 };
 
 __device__ __forceinline__ void count_solve(LocalStats& ls, unsigned int* hist_s, const SolveOut& o)
@@ -56,12 +56,16 @@ __device__ inline void flush_stats(LocalStats& ls, unsigned int* hist_s, DevStat
         ls.iterations += __shfl_down_sync(0xffffffffu, ls.iterations, off);
         ls.retries += __shfl_down_sync(0xffffffffu, ls.retries, off);
         ls.early += __shfl_down_sync(0xffffffffu, ls.early, off);
+        ls.warm_used += __shfl_down_sync(0xffffffffu, ls.warm_used, off);
+        ls.warm_fallback += __shfl_down_sync(0xffffffffu, ls.warm_fallback, off);
     }
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(&st->solves, ls.solves);
         atomicAdd(&st->iterations, ls.iterations);
         atomicAdd(&st->retries, ls.retries);
         atomicAdd(&st->early_exits, ls.early);
+        if (ls.warm_used) atomicAdd(&st->warm_used, ls.warm_used);
+        if (ls.warm_fallback) atomicAdd(&st->warm_fallback, ls.warm_fallback);
     }
     __syncthreads();
     if (threadIdx.x < 16 && hist_s[threadIdx.x]) atomicAdd(&st->hist[threadIdx.x], (unsigned long long)hist_s[threadIdx.x]);

@@ -22,6 +22,9 @@
 namespace tr {
 
 enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_DONE = 4 };
+// Warm-start phase of a solve: plain bracket, waiting for the learned depth
+// (set by the kernel before the next pass), or bracketing the learned depth.
+enum : int { W_PLAIN = 0, W_PENDING = 1, W_ACTIVE = 2 };
 
 // Everything a lane carries for one (reach, step) and the segment it solves.
 struct Lane {
@@ -36,9 +39,23 @@ struct Lane {
     SegP p;
     double qup, quc, qdp, ql;
     double h, h_0, Qj_0, qdc;
+    double dpp;            // previous depth (clamped at 0): the plain bracket's centre
     DepthEval e0;
-    int need0, iter, attempt, maxiter, total, retried;
+    int need0, iter, attempt, maxiter, total, retried, warm;
 };
+
+// The plain starting bracket from the previous depth (troute_mc_final.cu:193).
+__device__ __forceinline__ void plain_bracket(Lane& L, const Tol& tol)
+{
+    L.h = L.dpp * 1.33 + kMinDepth;
+    L.h_0 = L.dpp * 0.67;
+    L.Qj_0 = 0.0;
+    L.qdc = 0.0;
+    L.maxiter = tol.maxiter;
+    L.attempt = 0;
+    L.iter = 0;
+    L.need0 = 1;
+}
 
 // Starts segment L.i of the lane's reach; consecutive segments that exit early
 // (invalid parameters or no flow at all, troute_mc_final.cu:54-63) are stored
@@ -75,17 +92,11 @@ __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const 
             ++L.i;
             continue;
         }
-        const double depth = fmax(dpp, 0.0);
-        L.h = depth * 1.33 + kMinDepth;
-        L.h_0 = depth * 0.67;
-        L.Qj_0 = 0.0;
-        L.qdc = 0.0;
-        L.maxiter = run.tol.maxiter;
-        L.attempt = 0;
-        L.iter = 0;
+        L.dpp = fmax(dpp, 0.0);
+        plain_bracket(L, run.tol);
         L.total = 0;
         L.retried = 0;
-        L.need0 = 1;
+        L.warm = run.warm ? W_PENDING : W_PLAIN;
         return true;
     }
     return false;
@@ -97,7 +108,7 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
 {
     const Tol& tol = run.tol;
     const double dt = run.dt;
-    if (L.mode == L_SOLVE) {
+    if (L.mode == L_SOLVE && L.warm != W_PENDING) {
         const SegP& p = L.p;
         const double x = L.need0 ? L.h_0 : L.h;
         const double twl = p.bw + 2.0 * p.z * x;
@@ -178,10 +189,24 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                 L.e0 = e;
                 ++L.iter;
                 ++L.total;
-                const bool stop = (L.h < kMinDepth) || !(rerr > tol.rtol && aerr >= tol.atol && L.iter <= L.maxiter);
+                bool stop;
+                if (L.warm == W_ACTIVE) {
+                    // warm phase: accepted once the stop test passes at a depth of at
+                    // least kMinDepth; otherwise, after warm_k passes (or below
+                    // kMinDepth), the plain solve restarts from the previous depth
+                    const bool conv = !(rerr > tol.rtol && aerr >= tol.atol);
+                    stop = conv && L.h >= kMinDepth;
+                    if (!stop && (L.h < kMinDepth || L.iter >= run.warm_k)) {
+                        L.warm = W_PLAIN;
+                        ls.warm_fallback++;
+                        plain_bracket(L, tol);
+                    }
+                } else {
+                    stop = (L.h < kMinDepth) || !(rerr > tol.rtol && aerr >= tol.atol && L.iter <= L.maxiter);
+                }
                 if (stop) {
                     bool done = true;
-                    if (L.iter >= L.maxiter) {
+                    if (L.warm == W_PLAIN && L.iter >= L.maxiter) {
                         // widen the bracket (also after the last attempt, as the reference does)
                         L.h *= 1.33;
                         L.h_0 *= 0.67;
@@ -199,6 +224,18 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                         __stcg(net.q + L.s, L.qdc);
                         __stcg(net.d + L.s, L.h);
                         if (run.q_hist) __stcg(run.q_hist + (size_t)L.tau * (size_t)net.n_seg_int + L.s, L.qdc);
+                        if (run.pairs) {
+                            float* pr = run.pairs + ((size_t)L.tau * (size_t)net.n_seg_int + L.s) * 9;
+                            pr[0] = (float)L.qup;
+                            pr[1] = (float)L.quc;
+                            pr[2] = (float)L.qdp;
+                            pr[3] = (float)L.ql;
+                            pr[4] = (float)p.dx;
+                            pr[5] = (float)p.s0;
+                            pr[6] = (float)p.n_ch;
+                            pr[7] = (float)p.bw;
+                            pr[8] = (float)L.h;
+                        }
                         L.q_up_old = L.qdp;
                         L.q_up_new = L.qdc;
                         L.q_last = L.qdc;

@@ -51,7 +51,7 @@ extern "C" void troute_cfg_default(troute_cfg* cfg)
     cfg->atol = 0.01;
     cfg->maxiter = 100;
     cfg->attempts = 5;
-    cfg->warm_k = 4;
+    cfg->warm_k = 16;
 }
 
 namespace tr {
@@ -66,6 +66,9 @@ int check_cfg(const troute_cfg& c)
         return set_error(TROUTE_EINVAL, "cfg.threads_per_block must be a multiple of 32, at most 128");
     if (c.blocks_per_sm < 0 || c.wait_cycles < 0) return set_error(TROUTE_EINVAL, "negative cfg field");
     if (c.mapping < 0 || c.mapping > 3) return set_error(TROUTE_EINVAL, "cfg.mapping must be 0..3");
+    if (c.warm_start && c.mapping != 0 && c.mapping != 3)
+        return set_error(TROUTE_EINVAL, "cfg.warm_start needs mapping 3 (the ready-queue kernel)");
+    if (c.warm_start && (c.warm_k < 1 || c.warm_k > 100000)) return set_error(TROUTE_EINVAL, "cfg.warm_k out of range");
     return TROUTE_OK;
 }
 
@@ -188,6 +191,12 @@ struct troute_handle {
     int n_heads = 0, R_real = 0;
     DBuf<DevStats> stats;
     int hist_ts = 0;
+    // learned warm start and its training data
+    const troute_warm* warm_model = nullptr;
+    double warm_delta = 0.05;
+    DBuf<float> pairs;        // [n_ts][S_int][9]
+    DBuf<double> start_hist;  // [n_ts][S_int]
+    int pairs_ts = 0, start_ts = 0;
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -234,6 +243,7 @@ struct troute_handle {
         qlat_buf.release(); hist.release(); tile_off.release(); seg_map_d.release();
         reach_map_d.release(); wave_ptr.release(); wave_ptr_tail.release(); ticket.release(); stats.release();
         rq_ctr.release(); df_cnt.release(); df_rq.release(); df_heads.release(); df_rh.release();
+        pairs.release(); start_hist.release();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -260,7 +270,7 @@ static int launch_shape(troute_handle* H)
     H->mapping = H->cfg.mapping ? H->cfg.mapping : 3;
     if (H->mapping == 3) {
         H->threads = 128;
-        if ((rc = route_dataflow_occupancy(&bps))) return rc;
+        if ((rc = route_dataflow_occupancy(&bps, H->cfg.warm_start != 0))) return rc;
     } else if (H->mapping == 2) {
         H->threads = 128;
         if ((rc = route_pool_occupancy(&bps))) return rc;
@@ -835,7 +845,8 @@ static int plan_run(troute_handle* H, int n_ts, RunPlan* P)
 
 // Enqueues one chunk of n_ts steps (wave table `wave` already on the device).
 static int enqueue_chunk(troute_handle* H, const double* qlat_dev, int n_ts, const unsigned long long* wave,
-                         unsigned long long n_tickets, double* q_hist, cudaStream_t st)
+                         unsigned long long n_tickets, double* q_hist, float* pairs, double* start_hist,
+                         cudaStream_t st)
 {
     int rc;
     RunDev run;
@@ -852,6 +863,11 @@ static int enqueue_chunk(troute_handle* H, const double* qlat_dev, int n_ts, con
     run.wait_cycles = H->cfg.wait_cycles > 0 ? H->cfg.wait_cycles : 8000000000LL;
     run.tol = make_tol(H->cfg);
     run.q_hist = q_hist;
+    run.pairs = pairs;
+    run.start_hist = start_hist;
+    run.warm = H->cfg.warm_start ? 1 : 0;
+    run.warm_k = H->cfg.warm_k;
+    run.warm_delta = H->warm_delta;
     if ((rc = cuda_check(cudaMemsetAsync(H->ticket.p, 0, sizeof(unsigned long long), st), "memset"))) return rc;
     if (H->mapping == 3) {
         DataflowDev df;
@@ -865,7 +881,7 @@ static int enqueue_chunk(troute_handle* H, const double* qlat_dev, int n_ts, con
         df.n_heads = H->n_heads;
         df.continue_items = H->cfg.schedule_flags & 1;
         df.n_items = (unsigned long long)H->R_real * (unsigned long long)n_ts;
-        rc = launch_route_dataflow(H->net(), run, df, H->grid, st);
+        rc = launch_route_dataflow(H->net(), run, df, H->warm_model, H->grid, st);
     } else if (H->mapping == 2) {
         rc = launch_route_pool(H->net(), run, H->grid, H->threads, st);
     } else {
@@ -882,6 +898,14 @@ static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, const
 {
     int rc;
     if ((rc = cuda_check(cudaMemsetAsync(H->stats.p, 0, sizeof(DevStats), st), "memset"))) return rc;
+    const bool rec_pairs = H->cfg.record_pairs && H->pairs.p;
+    const bool rec_start = H->cfg.record_start && H->start_hist.p;
+    if (rec_pairs && (rc = cuda_check(cudaMemsetAsync(H->pairs.p, 0, (size_t)n_ts * H->S_int * 9 * sizeof(float), st),
+                                      "memset")))
+        return rc;
+    if (rec_start &&
+        (rc = cuda_check(cudaMemsetAsync(H->start_hist.p, 0, (size_t)n_ts * H->S_int * sizeof(double), st), "memset")))
+        return rc;
     if (timed && (rc = cuda_check(cudaEventRecord(H->ev0, st), "event"))) return rc;
     const int n_chunks = P.n_full + (P.rem ? 1 : 0);
     for (int c = 0; c < n_chunks; ++c) {
@@ -891,7 +915,10 @@ static int enqueue_run(troute_handle* H, const double* qlat_dev, int n_ts, const
         const unsigned long long* wave = tail ? H->wave_ptr_tail.p : H->wave_ptr.p;
         const unsigned long long nt = tail ? H->n_tickets_tail : H->n_tickets;
         double* qh = (H->cfg.record_history && H->hist.p) ? H->hist.p + (size_t)t0 * H->S_int : nullptr;
-        if ((rc = enqueue_chunk(H, qlat_dev + (size_t)t0 * (size_t)H->qlat_cols, len, wave, nt, qh, st))) return rc;
+        float* pr = rec_pairs ? H->pairs.p + (size_t)t0 * H->S_int * 9 : nullptr;
+        double* sh = rec_start ? H->start_hist.p + (size_t)t0 * H->S_int : nullptr;
+        if ((rc = enqueue_chunk(H, qlat_dev + (size_t)t0 * (size_t)H->qlat_cols, len, wave, nt, qh, pr, sh, st)))
+            return rc;
     }
     if (H->mapping >= 2 && (rc = launch_velocity(H->net(), st))) return rc;
     if (timed && (rc = cuda_check(cudaEventRecord(H->ev1, st), "event"))) return rc;
@@ -913,6 +940,8 @@ static int upload_waves(troute_handle* H, int len, DBuf<unsigned long long>& buf
 
 static int prepare_run(troute_handle* H, int n_ts, RunPlan* P)
 {
+    if (H->cfg.warm_start && !warm_ready(H->warm_model))
+        return set_error(TROUTE_ESTATE, "cfg.warm_start is set but no trained model is attached (troute_set_warm_start)");
     int rc = plan_run(H, n_ts, P);
     if (rc) return rc;
     if (H->mapping != 3) {
@@ -922,6 +951,14 @@ static int prepare_run(troute_handle* H, int n_ts, RunPlan* P)
     if (H->cfg.record_history) {
         if ((rc = H->hist.alloc((size_t)n_ts * H->S_int))) return rc;
         H->hist_ts = n_ts;
+    }
+    if (H->cfg.record_pairs) {
+        if ((rc = H->pairs.alloc((size_t)n_ts * H->S_int * 9))) return rc;
+        H->pairs_ts = n_ts;
+    }
+    if (H->cfg.record_start) {
+        if ((rc = H->start_hist.alloc((size_t)n_ts * H->S_int))) return rc;
+        H->start_ts = n_ts;
     }
     if (H->mapping == 3) {
         const size_t R = (size_t)std::max(1, H->R_int);
@@ -1051,6 +1088,44 @@ extern "C" int troute_graph_launch(troute_handle* h, void* stream)
     if (rc) return rc;
     h->steps_done += h->graph_n_ts;
     h->last_n_ts = 0;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_set_warm_start(troute_handle* h, const troute_warm* model, double delta)
+{
+    if (!h) return set_error(TROUTE_EINVAL, "null handle");
+    if (model && !warm_ready(model)) return set_error(TROUTE_ESTATE, "model has no trained weights");
+    if (model && !(delta > 0.0 && delta < 1.0)) return set_error(TROUTE_EINVAL, "delta must be in (0, 1)");
+    h->warm_model = model;
+    if (model) h->warm_delta = delta;
+    return TROUTE_OK;
+}
+
+extern "C" int troute_get_pairs(troute_handle* h, float* pairs_device, long long capacity, long long* n_pairs)
+{
+    if (!h || !n_pairs) return set_error(TROUTE_EINVAL, "null argument");
+    *n_pairs = 0;
+    if (!h->cfg.record_pairs || !h->pairs.p || h->pairs_ts == 0)
+        return set_error(TROUTE_ESTATE, "no pairs recorded (set cfg.record_pairs before the run)");
+    if (capacity > 0 && !pairs_device) return set_error(TROUTE_EINVAL, "null pair buffer");
+    return compact_pairs(h->pairs.p, (long long)h->pairs_ts * h->S_int, pairs_device, capacity, n_pairs, h->stream);
+}
+
+extern "C" int troute_get_start_history(troute_handle* h, double* start_hist, int n_ts)
+{
+    if (!h || !start_hist) return set_error(TROUTE_EINVAL, "null argument");
+    if (!h->cfg.record_start || !h->start_hist.p || n_ts != h->start_ts)
+        return set_error(TROUTE_ESTATE, "no starting depths of %d steps recorded (set cfg.record_start)", n_ts);
+    const size_t S = (size_t)h->S_user;
+    int rc;
+    for (int t = 0; t < n_ts; ++t) {
+        if ((rc = launch_gather(h->start_hist.p + (size_t)t * h->S_int, h->seg_map_d.p, (long long)S, h->tmp.p, h->stream)))
+            return rc;
+        if ((rc = cuda_check(cudaMemcpyAsync(start_hist + (size_t)t * S, h->tmp.p, S * sizeof(double),
+                                             cudaMemcpyDeviceToHost, h->stream), "start history download")))
+            return rc;
+        if ((rc = cuda_check(cudaStreamSynchronize(h->stream), "start history sync"))) return rc;
+    }
     return TROUTE_OK;
 }
 

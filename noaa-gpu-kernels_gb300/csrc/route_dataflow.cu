@@ -27,6 +27,7 @@
 // (wavefront_mc.cu:525-531), and the solve is lane_solver.cuh's, i.e. the
 // reference's arithmetic.
 #include "lane_solver.cuh"
+#include "warm.cuh"
 
 namespace tr {
 
@@ -98,12 +99,53 @@ __device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base,
     L.mode = begin_segment(L, net, run, ls, hist_s) ? L_SOLVE : L_DONE;
 }
 
-__global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df)
+// Learned starting depth for every lane of the warp whose solve waits for one
+// (W_PENDING): one tensor-core MLP evaluation for the whole warp, then the
+// bracket [p (1 - delta), p (1 + delta)] around the prediction p. A prediction
+// that is not a positive finite depth below 1e4 m leaves the plain bracket.
+__device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const WarmDev& m, const RunDev& run,
+                                                   long long n_seg_int, LocalStats& ls)
+{
+    const bool pend = (L.mode == L_SOLVE && L.warm == W_PENDING);
+    if (!__any_sync(0xffffffffu, pend)) return;
+    float f[kWIn];
+    if (pend) {
+        f[0] = warm_feature(L.qup, true, m.mu[0], m.sd[0]);
+        f[1] = warm_feature(L.quc, true, m.mu[1], m.sd[1]);
+        f[2] = warm_feature(L.qdp, true, m.mu[2], m.sd[2]);
+        f[3] = warm_feature(L.ql, true, m.mu[3], m.sd[3]);
+        f[4] = warm_feature(L.p.dx, false, m.mu[4], m.sd[4]);
+        f[5] = warm_feature(L.p.s0, false, m.mu[5], m.sd[5]);
+        f[6] = warm_feature(L.p.n_ch, false, m.mu[6], m.sd[6]);
+        f[7] = warm_feature(L.p.bw, false, m.mu[7], m.sd[7]);
+    } else {
+        for (int k = 0; k < kWIn; ++k) f[k] = 0.0f;
+    }
+    const float y = warm_mlp_warp(s, f, m.b3);
+    if (pend) {
+        const double pr = (double)expf(y * m.sd_y + m.mu_y);
+        if (pr > 0.0 && pr < 1.0e4) {
+            L.h = pr * (1.0 + run.warm_delta);
+            L.h_0 = pr * (1.0 - run.warm_delta);
+            L.warm = W_ACTIVE;
+            ls.warm_used++;
+            if (run.start_hist) __stcg(run.start_hist + (size_t)L.tau * (size_t)n_seg_int + L.s, pr);
+        } else {
+            L.warm = W_PLAIN;
+        }
+    }
+}
+
+template <bool WARM>
+__global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df, WarmDev wm)
 {
     __shared__ unsigned int hist_s[16];
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    WarmSmem& wsm = *reinterpret_cast<WarmSmem*>(dyn_smem);
     if (threadIdx.x < 16) hist_s[threadIdx.x] = 0;
+    if constexpr (WARM) warm_stage(wsm, wm);
     __syncthreads();
-    LocalStats ls = {0, 0, 0, 0};
+    LocalStats ls = {0, 0, 0, 0, 0, 0};
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt_df();
     const int t_base = __ldg(run.step_base);
@@ -212,6 +254,9 @@ __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev 
             }
         }
 
+        // ---- learned starting depths for solves that just began ----
+        if constexpr (WARM) warm_predict_lanes(L, wsm, wm, run, net.n_seg_int, ls);
+
         // ---- one depth evaluation per solving lane ----
         if (__any_sync(kFullMask, L.mode >= L_SOLVE)) lane_pass(L, net, run, ls, hist_s);
 
@@ -310,8 +355,10 @@ __global__ void dataflow_init_kernel(NetDev net, RunDev run, DataflowDev df)
     }
 }
 
-int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, int grid, void* stream)
+int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, const troute_warm* warm,
+                          int grid, void* stream)
 {
+    if (run.warm && !warm_ready(warm)) return set_error(TROUTE_ESTATE, "warm start requested without a trained model");
     if (df.n_items == 0) return TROUTE_OK;
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e;
@@ -327,15 +374,23 @@ int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDe
     if (ig > 4096) ig = 4096;
     if (ig < 1) ig = 1;
     dataflow_init_kernel<<<ig, 256, 0, st>>>(net, run, df);
-    route_dataflow_kernel<<<grid, 128, 0, st>>>(net, run, df);
+    if (run.warm) {
+        route_dataflow_kernel<true>
+            <<<grid, 128, sizeof(WarmSmem), st>>>(net, run, df, warm_device_view(warm, run.warm_delta, run.warm_k));
+    } else {
+        route_dataflow_kernel<false><<<grid, 128, 0, st>>>(net, run, df, WarmDev{});
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(TROUTE_ECUDA, "route_dataflow_kernel launch: %s", cudaGetErrorString(e));
     return TROUTE_OK;
 }
 
-int route_dataflow_occupancy(int* blocks_per_sm)
+int route_dataflow_occupancy(int* blocks_per_sm, bool warm)
 {
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, route_dataflow_kernel, 128, 0);
+    const cudaError_t e =
+        warm ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, route_dataflow_kernel<true>, 128,
+                                                             sizeof(WarmSmem))
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, route_dataflow_kernel<false>, 128, 0);
     if (e != cudaSuccess) return set_error(TROUTE_ECUDA, "occupancy query: %s", cudaGetErrorString(e));
     return TROUTE_OK;
 }

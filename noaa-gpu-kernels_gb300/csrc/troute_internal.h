@@ -113,6 +113,11 @@ struct RunDev {
     long long wait_cycles;
     Tol tol;
     double* q_hist;          // optional [n_ts][n_seg_int]
+    float* pairs;            // optional [n_ts][n_seg_int][9] training pairs (qup quc qdp ql dx s0 n bw depth)
+    double* start_hist;      // optional [n_ts][n_seg_int] learned starting depth of each solve (0: plain)
+    int warm;                // 1: solves start from the learned depth (dataflow kernel only)
+    int warm_k;              // passes of the warm phase before the plain fallback
+    double warm_delta;       // relative half-width of the warm bracket
 };
 
 // Ready-queue state of one run of the dataflow kernel (mapping 3).
@@ -139,8 +144,15 @@ int launch_route(const NetDev& net, const RunDev& run, int grid, int threads, vo
 int route_occupancy(int threads, int* blocks_per_sm);
 int launch_route_pool(const NetDev& net, const RunDev& run, int grid, int threads, void* stream);
 int route_pool_occupancy(int* blocks_per_sm);
-int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, int grid, void* stream);
-int route_dataflow_occupancy(int* blocks_per_sm);
+int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, const troute_warm* warm,
+                          int grid, void* stream);
+// Learned warm start (warm.cu): whether a model has weights on the device, and
+// the compaction of the dense per-solve pair records [n_rows][9] (rows with a
+// positive depth) into `out`, in row order; synchronous on `stream`.
+bool warm_ready(const troute_warm* w);
+int compact_pairs(const float* dense, long long n_rows, float* out, long long capacity, long long* n_valid,
+                  void* stream);
+int route_dataflow_occupancy(int* blocks_per_sm, bool warm);
 int launch_bump_steps(int* step_base, int n_ts, void* stream);
 int launch_fill_int(int* p, long long n, const int* value_dev, int value_host, void* stream);
 int launch_scatter(const double* src, const long long* map, long long n, double* dst,

@@ -60,7 +60,9 @@ class Cfg(C.Structure):
         ("mapping", C.c_int),
         ("schedule_flags", C.c_int),
         ("max_chunk_steps", C.c_int),
-        ("reserved", C.c_int * 4),
+        ("record_pairs", C.c_int),
+        ("record_start", C.c_int),
+        ("reserved", C.c_int * 2),
     ]
 
 
@@ -143,6 +145,16 @@ _SIGS = {
     "troute_get_history": ([_P, _P, _I], _I),
     "troute_checkpoint": ([_P, _P, _P], _I),
     "troute_restore": ([_P, _P, C.c_size_t], _I),
+    "troute_warm_create": ([_P, _U64], _I),
+    "troute_warm_destroy": ([_P], _I),
+    "troute_warm_get": ([_P, _P, _I], _I),
+    "troute_warm_set": ([_P, _P, _I], _I),
+    "troute_warm_fit": ([_P, _P, C.c_longlong, _I, _I, C.c_float, C.c_float, _U64, _P], _I),
+    "troute_warm_grad": ([_P, _P, _I, _P, _P], _I),
+    "troute_warm_predict": ([_P, _P, _I, _P], _I),
+    "troute_set_warm_start": ([_P, _P, _D], _I),
+    "troute_get_pairs": ([_P, _P, C.c_longlong, _P], _I),
+    "troute_get_start_history": ([_P, _P, _I], _I),
     "troute_debug_timeout_probe": ([C.c_longlong], _I),
     "troute_debug_pow": ([_P, _I, _P], _I),
     "troute_levels": ([_I, _P, _P, _P, _P, _P, _P], _I),
@@ -439,6 +451,24 @@ class Network:
         _check(lib().troute_get_history(self._h, _ptr(out), int(n_ts)))
         return out
 
+    def set_warm_start(self, model: "WarmModel | None", delta: float = 0.05):
+        """Attaches a trained model (None detaches); runs use it with cfg.warm_start = 1."""
+        self._warm = model
+        _check(lib().troute_set_warm_start(self._h, None if model is None else model._h, float(delta)))
+
+    def pairs(self, out_dev_ptr: int = 0, capacity: int = 0) -> int:
+        """Training pairs of the last run (cfg.record_pairs): copies up to
+        `capacity` into the device buffer at out_dev_ptr; returns how many exist."""
+        n = C.c_longlong()
+        _check(lib().troute_get_pairs(self._h, C.c_void_p(out_dev_ptr or None), int(capacity), C.byref(n)))
+        return n.value
+
+    def start_history(self, n_ts: int):
+        """Learned starting depth of every solve of the last run (cfg.record_start), 0 = plain start."""
+        out = np.zeros((n_ts, self.n_segments))
+        _check(lib().troute_get_start_history(self._h, _ptr(out), int(n_ts)))
+        return out
+
     def checkpoint(self) -> bytes:
         n = C.c_size_t(0)
         _check(lib().troute_checkpoint(self._h, None, C.byref(n)))
@@ -449,6 +479,68 @@ class Network:
     def restore(self, blob: bytes):
         buf = C.create_string_buffer(blob, len(blob))
         _check(lib().troute_restore(self._h, buf, len(blob)))
+
+
+WARM_NPARAMS = 4801
+WARM_NSTATE = WARM_NPARAMS + 18
+PAIR_FLOATS = 9
+
+
+class WarmModel:
+    """The learned warm start's MLP (8 -> 64 -> 64 -> 1, SiLU), held by the library.
+
+    State vector (get_state / set_state): W1 [64][8], b1 [64], W2 [64][64],
+    b2 [64], w3 [64], b3, then mu[8], sd[8], mu_y, sd_y (standardisation of
+    the log inputs and log depth)."""
+
+    def __init__(self, seed: int = 0):
+        self._h = C.c_void_p()
+        _check(lib().troute_warm_create(C.byref(self._h), C.c_uint64(seed)))
+
+    def close(self):
+        if self._h:
+            lib().troute_warm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_state(self) -> np.ndarray:
+        out = np.zeros(WARM_NSTATE, np.float32)
+        _check(lib().troute_warm_get(self._h, _ptr(out), out.size))
+        return out
+
+    def set_state(self, state):
+        st = np.ascontiguousarray(state, np.float32)
+        if st.size != WARM_NSTATE:
+            raise ValueError(f"state must hold {WARM_NSTATE} floats")
+        _check(lib().troute_warm_set(self._h, _ptr(st), st.size))
+
+    def fit(self, pairs_dev_ptr: int, n_pairs: int, epochs: int = 4, batch: int = 8192, lr: float = 2e-3,
+            weight_decay: float = 1e-4, seed: int = 0) -> np.ndarray:
+        """Trains on device-resident pairs [n_pairs][9]; returns the loss of each epoch."""
+        loss = np.zeros(epochs, np.float32)
+        _check(lib().troute_warm_fit(self._h, C.c_void_p(pairs_dev_ptr), int(n_pairs), int(epochs), int(batch),
+                                     float(lr), float(weight_decay), C.c_uint64(seed), _ptr(loss)))
+        return loss
+
+    def grad(self, pairs) -> tuple:
+        """(gradient [WARM_NPARAMS], loss) of mean (err^2)/2 over host pairs [n][9]."""
+        pr = np.ascontiguousarray(pairs, np.float32).reshape(-1, PAIR_FLOATS)
+        g = np.zeros(WARM_NPARAMS, np.float32)
+        loss = C.c_double()
+        _check(lib().troute_warm_grad(self._h, _ptr(pr), pr.shape[0], _ptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def predict(self, inputs) -> np.ndarray:
+        """Predicted depths for host rows [n][8] (qup quc qdp ql dx s0 n bw), tensor-core path."""
+        x = np.ascontiguousarray(inputs, np.float32).reshape(-1, 8)
+        out = np.zeros(x.shape[0])
+        _check(lib().troute_warm_predict(self._h, _ptr(x), x.shape[0], _ptr(out)))
+        return out
 
 
 def route_tree(topo: dict, params, qlat_ts, qdp0, dp0, reach_last0=None, dt: float = 300.0, cfg: Cfg | None = None,

@@ -143,17 +143,95 @@ static double manning_q(const geo* g, double n_ch, double ncc, double s0)
            P23(g->R) * sqrt(s0);
 }
 
-double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
-                       const oracle_chparams* p, double depthp,
-                       const oracle_tol* tol,
-                       double* depthc, double* velc, int* iters)
+/* State of one secant solve between passes. */
+typedef struct secant {
+    double h, h_0, Qj_0, C1, C2, C3, C4, rerr, aerr;
+} secant;
+
+/* One pass of the secant loop body, troute_mc_final.cu:198-237: residuals at
+ * h_0 and h, the secant update and the errors. */
+static void secant_pass(secant* S, double dt, double qup, double quc, double qdp, double ql,
+                        const oracle_chparams* p, double z, double bfd)
 {
-    const double bw = p->bw, tw = p->tw, twcc = p->twcc, n_ch = p->n_ch, ncc = p->ncc;
+    const double bw = p->bw, twcc = p->twcc, n_ch = p->n_ch, ncc = p->ncc;
     const double s0 = p->s0, dx = p->dx;
+    double h = S->h, h_0 = S->h_0;
+    /* lower point h_0, :200-214 */
+    geo g0;
+    channel_geometry(h_0, bfd, bw, twcc, z, &g0);
+    const double Ck0 = celerity(h_0, &g0, s0, n_ch, bw, z);
+    const double Km0 = (Ck0 > 0.0) ? fmax(dt, dx / Ck0) : dt;
+    const double twu0 = (h_0 > bfd && twcc > 0.0) ? twcc : g0.twl;
+    const double X0 = (Ck0 > 0.0 && twu0 * s0 * Ck0 * dx > 0.0)
+                          ? fmin(0.5, fmax(0.0, 0.5 * (1.0 - S->Qj_0 / (2.0 * twu0 * s0 * Ck0 * dx))))
+                          : 0.5;
+    double D0 = Km0 * (1.0 - X0) + dt / 2.0;
+    if (D0 == 0.0) D0 = 1.0;
+    const double c1 = (Km0 * X0 + dt / 2.0) / D0;
+    const double c2 = (dt / 2.0 - Km0 * X0) / D0;
+    const double c3 = (Km0 * (1.0 - X0) - dt / 2.0) / D0;
+    const double c4 = (ql * dt) / D0;
+    const double qmc0 = c1 * qup + c2 * quc + c3 * qdp + c4;
+    const double Qj_0 = qmc0 - manning_q(&g0, n_ch, ncc, s0);
+
+    /* upper point h, :216-231; X is clamped to [0.25, 0.5] here and uses the
+     * h_0 coefficients in its numerator */
+    geo g1;
+    channel_geometry(h, bfd, bw, twcc, z, &g1);
+    const double Ck1 = celerity(h, &g1, s0, n_ch, bw, z);
+    const double Km1 = (Ck1 > 0.0) ? fmax(dt, dx / Ck1) : dt;
+    const double twu1 = (h > bfd && twcc > 0.0) ? twcc : g1.twl;
+    const double X = (Ck1 > 0.0 && twu1 * s0 * Ck1 * dx > 0.0)
+                         ? fmin(0.5, fmax(0.25, 0.5 * (1.0 - qmc0 / (2.0 * twu1 * s0 * Ck1 * dx))))
+                         : 0.5;
+    double D1 = Km1 * (1.0 - X) + dt / 2.0;
+    if (D1 == 0.0) D1 = 1.0;
+    const double C1 = (Km1 * X + dt / 2.0) / D1;
+    const double C2 = (dt / 2.0 - Km1 * X) / D1;
+    const double C3 = (Km1 * (1.0 - X) - dt / 2.0) / D1;
+    double C4 = (ql * dt) / D1;
+    if (C4 < 0.0 && fabs(C4) > C1 * qup + C2 * quc + C3 * qdp)
+        C4 = -(C1 * qup + C2 * quc + C3 * qdp);
+    const double Qj = (C1 * qup + C2 * quc + C3 * qdp + C4) - manning_q(&g1, n_ch, ncc, s0);
+
+    /* secant update, :233-237 */
+    double h_1 = (Qj_0 - Qj != 0.0) ? h - (Qj * (h_0 - h)) / (Qj_0 - Qj) : h;
+    if (h_1 < 0.0) h_1 = h;
+    if (h > 0.0) {
+        S->rerr = fabs((h_1 - h) / h);
+        S->aerr = fabs(h_1 - h);
+    } else {
+        S->rerr = 0.0;
+        S->aerr = 0.9;
+    }
+    S->h_0 = fmax(0.0, h);
+    S->h = fmax(0.0, h_1);
+    S->Qj_0 = Qj_0;
+    S->C1 = C1;
+    S->C2 = C2;
+    S->C3 = C3;
+    S->C4 = C4;
+}
+
+/* The solve with an optional learned starting depth. start > 0: the first
+ * phase brackets [start (1 - delta), start (1 + delta)] and runs at most
+ * warm_k passes; it is accepted when the stop test (rerr <= rtol or
+ * aerr < atol) passes with h >= MINDEPTH, otherwise the solve restarts as the
+ * plain solve from the previous depth (a fallback; its passes still count).
+ * start <= 0: the plain solve. *warm_state: 0 plain, 1 warm start accepted,
+ * 2 fallback. */
+static double mc_solve_core(double dt, double qup, double quc, double qdp, double ql,
+                            const oracle_chparams* p, double depthp, const oracle_tol* tol,
+                            double start, double delta, int warm_k,
+                            double* depthc, double* velc, int* iters, int* warm_state)
+{
+    const double bw = p->bw, tw = p->tw, n_ch = p->n_ch;
+    const double s0 = p->s0;
     /* side slope and bankfull depth, :181-183 */
     const double z = (p->cs == 0.0) ? 1.0 : 1.0 / p->cs;
     const double bfd = (bw > tw) ? bw / 0.00001 : (bw == tw) ? bw / (2.0 * z) : (tw - bw) / (2.0 * z);
     *iters = 0;
+    *warm_state = 0;
 
     /* invalid parameters or no flow at all: zero outputs, :187-190 */
     if (n_ch <= 0.0 || s0 <= 0.0 || z <= 0.0 || bw <= 0.0 ||
@@ -163,82 +241,56 @@ double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
         return 0.0;
     }
 
-    const double depth = fmax(depthp, 0.0);
-    double h = depth * 1.33 + MINDEPTH; /* upper secant start, :193 */
-    double h_0 = depth * 0.67;          /* lower secant start */
-    double C1 = 0.0, C2 = 0.0, C3 = 0.0, C4 = 0.0, X = 0.25;
-    double Qj_0 = 0.0, Qj;
-    int maxiter = tol->maxiter;
+    secant S;
+    memset(&S, 0, sizeof S);
     int total = 0;
-
-    for (int attempt = 0; attempt < tol->attempts; attempt++) {
-        double aerr = 0.01, rerr = 1.0;
-        int iter = 0;
-        int first = 1; /* the first pass of every attempt always runs */
-        while (first || (rerr > tol->rtol && aerr >= tol->atol && iter <= maxiter)) {
-            first = 0;
-            /* lower point h_0, :200-214 */
-            geo g0;
-            channel_geometry(h_0, bfd, bw, twcc, z, &g0);
-            const double Ck0 = celerity(h_0, &g0, s0, n_ch, bw, z);
-            const double Km0 = (Ck0 > 0.0) ? fmax(dt, dx / Ck0) : dt;
-            const double twu0 = (h_0 > bfd && twcc > 0.0) ? twcc : g0.twl;
-            const double X0 = (Ck0 > 0.0 && twu0 * s0 * Ck0 * dx > 0.0)
-                                  ? fmin(0.5, fmax(0.0, 0.5 * (1.0 - Qj_0 / (2.0 * twu0 * s0 * Ck0 * dx))))
-                                  : 0.5;
-            double D0 = Km0 * (1.0 - X0) + dt / 2.0;
-            if (D0 == 0.0) D0 = 1.0;
-            const double c1 = (Km0 * X0 + dt / 2.0) / D0;
-            const double c2 = (dt / 2.0 - Km0 * X0) / D0;
-            const double c3 = (Km0 * (1.0 - X0) - dt / 2.0) / D0;
-            const double c4 = (ql * dt) / D0;
-            const double qmc0 = c1 * qup + c2 * quc + c3 * qdp + c4;
-            Qj_0 = qmc0 - manning_q(&g0, n_ch, ncc, s0);
-
-            /* upper point h, :216-231; X is clamped to [0.25, 0.5] here and
-             * uses the h_0 coefficients in its numerator */
-            geo g1;
-            channel_geometry(h, bfd, bw, twcc, z, &g1);
-            const double Ck1 = celerity(h, &g1, s0, n_ch, bw, z);
-            const double Km1 = (Ck1 > 0.0) ? fmax(dt, dx / Ck1) : dt;
-            const double twu1 = (h > bfd && twcc > 0.0) ? twcc : g1.twl;
-            X = (Ck1 > 0.0 && twu1 * s0 * Ck1 * dx > 0.0)
-                    ? fmin(0.5, fmax(0.25, 0.5 * (1.0 - qmc0 / (2.0 * twu1 * s0 * Ck1 * dx))))
-                    : 0.5;
-            double D1 = Km1 * (1.0 - X) + dt / 2.0;
-            if (D1 == 0.0) D1 = 1.0;
-            C1 = (Km1 * X + dt / 2.0) / D1;
-            C2 = (dt / 2.0 - Km1 * X) / D1;
-            C3 = (Km1 * (1.0 - X) - dt / 2.0) / D1;
-            C4 = (ql * dt) / D1;
-            if (C4 < 0.0 && fabs(C4) > C1 * qup + C2 * quc + C3 * qdp)
-                C4 = -(C1 * qup + C2 * quc + C3 * qdp);
-            Qj = (C1 * qup + C2 * quc + C3 * qdp + C4) - manning_q(&g1, n_ch, ncc, s0);
-
-            /* secant update, :233-237 */
-            double h_1 = (Qj_0 - Qj != 0.0) ? h - (Qj * (h_0 - h)) / (Qj_0 - Qj) : h;
-            if (h_1 < 0.0) h_1 = h;
-            if (h > 0.0) {
-                rerr = fabs((h_1 - h) / h);
-                aerr = fabs(h_1 - h);
-            } else {
-                rerr = 0.0;
-                aerr = 0.9;
-            }
-            h_0 = fmax(0.0, h);
-            h = fmax(0.0, h_1);
+    int solved = 0;
+    if (start > 0.0) {
+        *warm_state = 1;
+        S.h = start * (1.0 + delta);
+        S.h_0 = start * (1.0 - delta);
+        S.Qj_0 = 0.0;
+        for (int iter = 0;;) {
+            secant_pass(&S, dt, qup, quc, qdp, ql, p, z, bfd);
             iter++;
             total++;
-            if (h < MINDEPTH) break;
+            if (S.h < MINDEPTH) break;
+            if (!(S.rerr > tol->rtol && S.aerr >= tol->atol)) {
+                solved = 1;
+                break;
+            }
+            if (iter >= warm_k) break;
         }
-        if (iter < maxiter) break;
-        /* widen the bracket and allow more iterations, :240 */
-        h *= 1.33;
-        h_0 *= 0.67;
-        maxiter += 25;
+        if (!solved) *warm_state = 2;
+    }
+    if (!solved) {
+        const double depth = fmax(depthp, 0.0);
+        S.h = depth * 1.33 + MINDEPTH; /* upper secant start, :193 */
+        S.h_0 = depth * 0.67;          /* lower secant start */
+        S.Qj_0 = 0.0;
+        int maxiter = tol->maxiter;
+        for (int attempt = 0; attempt < tol->attempts; attempt++) {
+            int iter = 0;
+            S.aerr = 0.01;
+            S.rerr = 1.0;
+            int first = 1; /* the first pass of every attempt always runs */
+            while (first || (S.rerr > tol->rtol && S.aerr >= tol->atol && iter <= maxiter)) {
+                first = 0;
+                secant_pass(&S, dt, qup, quc, qdp, ql, p, z, bfd);
+                iter++;
+                total++;
+                if (S.h < MINDEPTH) break;
+            }
+            if (iter < maxiter) break;
+            /* widen the bracket and allow more iterations, :240 */
+            S.h *= 1.33;
+            S.h_0 *= 0.67;
+            maxiter += 25;
+        }
     }
 
     /* outflow with the negative-flow fallbacks, :242-244 */
+    const double C1 = S.C1, C2 = S.C2, C3 = S.C3, C4 = S.C4;
     double qdc;
     const double Qmc = C1 * qup + C2 * quc + C3 * qdp + C4;
     if (Qmc < 0.0) {
@@ -251,6 +303,7 @@ double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
     }
 
     /* velocity from the trapezoid-only hydraulic radius, :245-248 */
+    const double h = S.h;
     const double twl = bw + 2.0 * z * h;
     double Rv = (h * (bw + twl) / 2.0) /
                 (bw + 2.0 * sqrt(((twl - bw) / 2.0) * ((twl - bw) / 2.0) + h * h));
@@ -259,6 +312,24 @@ double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
     *depthc = h;
     *iters = total;
     return qdc;
+}
+
+double oracle_mc_solve(double dt, double qup, double quc, double qdp, double ql,
+                       const oracle_chparams* p, double depthp,
+                       const oracle_tol* tol,
+                       double* depthc, double* velc, int* iters)
+{
+    int ws;
+    return mc_solve_core(dt, qup, quc, qdp, ql, p, depthp, tol, 0.0, 0.0, 0, depthc, velc, iters, &ws);
+}
+
+double oracle_mc_solve_warm(double dt, double qup, double quc, double qdp, double ql,
+                            const oracle_chparams* p, double depthp, const oracle_tol* tol,
+                            double start, double delta, int warm_k,
+                            double* depthc, double* velc, int* iters, int* warm_state)
+{
+    return mc_solve_core(dt, qup, quc, qdp, ql, p, depthp, tol, start, delta, warm_k, depthc, velc, iters,
+                         warm_state);
 }
 
 void oracle_cpu_mc(const oracle_chparams* p, const double* ql,
@@ -302,7 +373,11 @@ typedef struct tree_job {
     const oracle_tol* tol;
     double *q[2], *d[2], *v, *rl[2];
     double* q_hist;
+    double* d_hist;
     int* it_hist;
+    const double* warm_start;
+    double warm_delta;
+    int warm_k;
     int n_threads;
     pthread_barrier_t barrier;
 } tree_job;
@@ -310,10 +385,10 @@ typedef struct tree_job {
 typedef struct tree_worker {
     tree_job* job;
     int rank;
-    long long iters;
+    long long iters, warm_used, warm_fallback;
 } tree_worker;
 
-static void route_reach(tree_job* J, int r, int t, long long* iters)
+static void route_reach(tree_job* J, int r, int t, tree_worker* W)
 {
     const int prev = t & 1, cur = (t + 1) & 1;
     const double* qlat = J->qlat_ts + (size_t)t * (size_t)J->n_segments;
@@ -333,17 +408,23 @@ static void route_reach(tree_job* J, int r, int t, long long* iters)
         const double qup = (i == 0) ? qup_head : J->q[prev][s - 1];
         const double quc = (i == 0) ? quc_head : quc_next;
         double dc, vc;
-        int it;
-        const double q = oracle_mc_solve(J->dt, qup, quc, J->q[prev][s], qlat[s], &J->params[s],
-                                         J->d[prev][s], J->tol, &dc, &vc, &it);
+        int it, ws;
+        const size_t ts = (size_t)t * (size_t)J->n_segments + s;
+        const double start = J->warm_start ? J->warm_start[ts] : 0.0;
+        const double q = mc_solve_core(J->dt, qup, quc, J->q[prev][s], qlat[s], &J->params[s],
+                                       J->d[prev][s], J->tol, start, J->warm_delta, J->warm_k,
+                                       &dc, &vc, &it, &ws);
         J->q[cur][s] = q;
         J->d[cur][s] = dc;
         J->v[s] = vc;
-        if (J->q_hist) J->q_hist[(size_t)t * (size_t)J->n_segments + s] = q;
-        if (J->it_hist) J->it_hist[(size_t)t * (size_t)J->n_segments + s] = it;
+        if (J->q_hist) J->q_hist[ts] = q;
+        if (J->d_hist) J->d_hist[ts] = dc;
+        if (J->it_hist) J->it_hist[ts] = it;
         quc_next = q;
         q_last = q;
-        *iters += it;
+        W->iters += it;
+        W->warm_used += (ws != 0);
+        W->warm_fallback += (ws == 2);
     }
     J->rl[cur][r] = q_last;
 }
@@ -359,7 +440,7 @@ static void* tree_worker_main(void* arg)
             const int per = (n + J->n_threads - 1) / J->n_threads;
             const int b = lb + W->rank * per;
             const int e = (b + per < le) ? b + per : le;
-            for (int ii = b; ii < e; ++ii) route_reach(J, J->level_reach[ii], t, &W->iters);
+            for (int ii = b; ii < e; ++ii) route_reach(J, J->level_reach[ii], t, W);
             if (J->n_threads > 1) pthread_barrier_wait(&J->barrier);
         }
     }
@@ -383,7 +464,7 @@ int oracle_route_tree(const int* reach_seg_start, const int* reach_seg_len,
                                 NULL, iters_total, n_threads);
 }
 
-int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
+int oracle_route_tree_ex(const int* reach_seg_start, const int* reach_seg_len,
                          const int* reach_up_ptr, const int* reach_up_idx,
                          const int* level_ptr, const int* level_reach,
                          int n_reaches, int n_levels, int n_segments,
@@ -391,9 +472,11 @@ int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
                          const double* qdp0, const double* dp0, const double* reach_last0,
                          int n_ts, double dt, const oracle_tol* tol,
                          double* q_out, double* d_out, double* v_out,
-                         double* reach_last_out, double* q_hist, int* it_hist,
-                         long long* iters_total, int n_threads)
+                         double* reach_last_out, oracle_tree_opts* opts)
 {
+    double* q_hist = opts->q_hist;
+    int* it_hist = opts->it_hist;
+    int n_threads = opts->n_threads;
     if (n_reaches < 0 || n_segments < 0 || n_levels < 0 || n_ts < 0) return 1;
     if (n_threads < 1) n_threads = 1;
     tree_job J;
@@ -414,6 +497,10 @@ int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
     J.tol = tol;
     J.q_hist = q_hist;
     J.it_hist = it_hist;
+    J.d_hist = opts->d_hist;
+    J.warm_start = opts->warm_start;
+    J.warm_delta = opts->warm_delta;
+    J.warm_k = opts->warm_k;
     J.n_threads = n_threads;
     const size_t S = (size_t)n_segments, R = (size_t)n_reaches;
     double* buf = (double*)calloc(4 * S + 2 * R + 1, sizeof(double));
@@ -430,11 +517,13 @@ int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
     memcpy(J.rl[0], reach_last0, R * sizeof(double));
     memset(v_out, 0, S * sizeof(double));
 
-    long long total = 0;
+    long long total = 0, used = 0, fell = 0;
     if (n_threads == 1) {
-        tree_worker W = {&J, 0, 0};
+        tree_worker W = {&J, 0, 0, 0, 0};
         tree_worker_main(&W);
         total = W.iters;
+        used = W.warm_used;
+        fell = W.warm_fallback;
     } else {
         pthread_barrier_init(&J.barrier, NULL, (unsigned)n_threads);
         tree_worker* W = (tree_worker*)calloc((size_t)n_threads, sizeof(tree_worker));
@@ -446,7 +535,11 @@ int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
         }
         tree_worker_main(&W[0]);
         for (int i = 1; i < n_threads; ++i) pthread_join(th[i], NULL);
-        for (int i = 0; i < n_threads; ++i) total += W[i].iters;
+        for (int i = 0; i < n_threads; ++i) {
+            total += W[i].iters;
+            used += W[i].warm_used;
+            fell += W[i].warm_fallback;
+        }
         pthread_barrier_destroy(&J.barrier);
         free(W);
         free(th);
@@ -455,7 +548,32 @@ int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
     memcpy(q_out, J.q[fin], S * sizeof(double));
     memcpy(d_out, J.d[fin], S * sizeof(double));
     memcpy(reach_last_out, J.rl[fin], R * sizeof(double));
-    if (iters_total) *iters_total = total;
+    opts->iters_total = total;
+    opts->warm_used = used;
+    opts->warm_fallback = fell;
     free(buf);
     return 0;
+}
+
+int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
+                         const int* reach_up_ptr, const int* reach_up_idx,
+                         const int* level_ptr, const int* level_reach,
+                         int n_reaches, int n_levels, int n_segments,
+                         const oracle_chparams* params, const double* qlat_ts,
+                         const double* qdp0, const double* dp0, const double* reach_last0,
+                         int n_ts, double dt, const oracle_tol* tol,
+                         double* q_out, double* d_out, double* v_out,
+                         double* reach_last_out, double* q_hist, int* it_hist,
+                         long long* iters_total, int n_threads)
+{
+    oracle_tree_opts o;
+    memset(&o, 0, sizeof o);
+    o.q_hist = q_hist;
+    o.it_hist = it_hist;
+    o.n_threads = n_threads;
+    const int rc = oracle_route_tree_ex(reach_seg_start, reach_seg_len, reach_up_ptr, reach_up_idx, level_ptr,
+                                        level_reach, n_reaches, n_levels, n_segments, params, qlat_ts, qdp0, dp0,
+                                        reach_last0, n_ts, dt, tol, q_out, d_out, v_out, reach_last_out, &o);
+    if (iters_total) *iters_total = o.iters_total;
+    return rc;
 }

@@ -90,6 +90,41 @@ int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
                          double* reach_last_out, double* q_hist, int* it_hist,
                          long long* iters_total, int n_threads);
 
+/* The solve with a learned starting depth. start > 0: the first phase
+ * brackets [start (1 - delta), start (1 + delta)] and gets at most warm_k
+ * passes; it is accepted when the stop test passes with depth >= 0.01,
+ * otherwise the plain solve runs from depthp (a fallback; all passes count in
+ * *iters). start <= 0: the plain solve. *warm_state: 0 plain, 1 accepted,
+ * 2 fallback. */
+double oracle_mc_solve_warm(double dt, double qup, double quc, double qdp, double ql,
+                            const oracle_chparams* p, double depthp, const oracle_tol* tol,
+                            double start, double delta, int warm_k,
+                            double* depthc, double* velc, int* iters, int* warm_state);
+
+/* Options and per-solve outputs of oracle_route_tree_ex. */
+typedef struct oracle_tree_opts {
+    const double* warm_start; /* [n_ts][n_segments] starting depth per solve (<= 0: plain), or NULL */
+    double warm_delta;        /* relative half-width of the warm bracket */
+    int warm_k;               /* passes of the warm phase */
+    int n_threads;
+    double* q_hist;           /* [n_ts][n_segments] discharge, or NULL */
+    double* d_hist;           /* [n_ts][n_segments] depth, or NULL */
+    int* it_hist;             /* [n_ts][n_segments] secant passes, or NULL */
+    long long iters_total;    /* out */
+    long long warm_used;      /* out: solves started from warm_start */
+    long long warm_fallback;  /* out: of those, solves that fell back */
+} oracle_tree_opts;
+
+int oracle_route_tree_ex(const int* reach_seg_start, const int* reach_seg_len,
+                         const int* reach_up_ptr, const int* reach_up_idx,
+                         const int* level_ptr, const int* level_reach,
+                         int n_reaches, int n_levels, int n_segments,
+                         const oracle_chparams* params, const double* qlat_ts,
+                         const double* qdp0, const double* dp0, const double* reach_last0,
+                         int n_ts, double dt, const oracle_tol* tol,
+                         double* q_out, double* d_out, double* v_out,
+                         double* reach_last_out, oracle_tree_opts* opts);
+
 #ifdef __cplusplus
 }
 #endif

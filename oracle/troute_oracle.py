@@ -64,6 +64,11 @@ def oracle():
         L.oracle_route_tree.restype = C.c_int
         L.oracle_mc_solve.argtypes = [C.c_double] * 5 + [_P, C.c_double, _P, _P, _P, _P]
         L.oracle_mc_solve.restype = C.c_double
+        L.oracle_route_tree_ex.argtypes = [_P] * 6 + [C.c_int] * 3 + [_P] * 5 + [C.c_int, C.c_double, _P] + [_P] * 5
+        L.oracle_route_tree_ex.restype = C.c_int
+        L.oracle_mc_solve_warm.argtypes = ([C.c_double] * 5 + [_P, C.c_double, _P, C.c_double, C.c_double, C.c_int]
+                                           + [_P] * 4)
+        L.oracle_mc_solve_warm.restype = C.c_double
         L.oracle_set_pow_mode.argtypes = [C.c_int]
         L.oracle_set_pow_mode.restype = None
         L.oracle_pow23_53.argtypes = [C.c_double, _P, _P]
@@ -145,9 +150,20 @@ def mc_solve(dt, qup, quc, qdp, ql, p_record, depthp, tol=REF_TOL):
     return q, d.value, v.value, it.value
 
 
+class TreeOpts(C.Structure):
+    _fields_ = [("warm_start", C.c_void_p), ("warm_delta", C.c_double), ("warm_k", C.c_int), ("n_threads", C.c_int),
+                ("q_hist", C.c_void_p), ("d_hist", C.c_void_p), ("it_hist", C.c_void_p),
+                ("iters_total", C.c_longlong), ("warm_used", C.c_longlong), ("warm_fallback", C.c_longlong)]
+
+
 def route_tree(topo, params, qlat_ts, qdp0, dp0, reach_last0, dt=300.0, tol=REF_TOL, history=False, threads=1,
-               level_ptr=None, level_reach=None):
-    """Oracle tree routing (cpu_wavefront_fp64 semantics, FP64 inputs)."""
+               level_ptr=None, level_reach=None, warm_start=None, warm_delta=0.0, warm_k=0, depth_history=False,
+               iter_history=False):
+    """Oracle tree routing (cpu_wavefront_fp64 semantics, FP64 inputs).
+
+    warm_start: optional [n_ts][n_segments] starting depth of every solve
+    (<= 0: plain start), with the warm bracket half-width warm_delta and
+    warm_k passes before the plain fallback (oracle_mc_solve_warm)."""
     seg_start = np.ascontiguousarray(topo["reach_seg_start"], np.int32)
     seg_len = np.ascontiguousarray(topo["reach_seg_len"], np.int32)
     up_ptr = np.ascontiguousarray(topo["reach_up_ptr"], np.int32)
@@ -163,18 +179,40 @@ def route_tree(topo, params, qlat_ts, qdp0, dp0, reach_last0, dt=300.0, tol=REF_
     q0, d0, r0 = (np.ascontiguousarray(x, np.float64) for x in (qdp0, dp0, reach_last0))
     q, d, v, rl = np.zeros(S), np.zeros(S), np.zeros(S), np.zeros(R)
     hist = np.zeros((T, S)) if history else None
-    it = C.c_longlong()
+    dhist = np.zeros((T, S)) if depth_history else None
+    ihist = np.zeros((T, S), np.int32) if iter_history else None
+    ws = None
+    if warm_start is not None:
+        ws = np.ascontiguousarray(warm_start, np.float64)
+        if ws.shape != (T, S):
+            raise ValueError(f"warm_start must be [{T}][{S}]")
+    o = TreeOpts(_ptr(ws), float(warm_delta), int(warm_k), int(threads), _ptr(hist), _ptr(dhist), _ptr(ihist), 0, 0, 0)
     t = _tol(tol)
-    rc = oracle().oracle_route_tree(_ptr(seg_start), _ptr(seg_len), _ptr(up_ptr), _ptr(up_idx), _ptr(level_ptr),
-                                    _ptr(level_reach), R, level_ptr.size - 1, S, _ptr(p), _ptr(ql), _ptr(q0), _ptr(d0),
-                                    _ptr(r0), T, float(dt), C.byref(t), _ptr(q), _ptr(d), _ptr(v), _ptr(rl),
-                                    _ptr(hist), C.byref(it), int(threads))
+    rc = oracle().oracle_route_tree_ex(_ptr(seg_start), _ptr(seg_len), _ptr(up_ptr), _ptr(up_idx), _ptr(level_ptr),
+                                       _ptr(level_reach), R, level_ptr.size - 1, S, _ptr(p), _ptr(ql), _ptr(q0),
+                                       _ptr(d0), _ptr(r0), T, float(dt), C.byref(t), _ptr(q), _ptr(d), _ptr(v),
+                                       _ptr(rl), C.byref(o))
     if rc != 0:
         raise RuntimeError(f"oracle_route_tree failed: {rc}")
-    out = {"q": q, "d": d, "v": v, "reach_last": rl, "iterations": it.value}
+    out = {"q": q, "d": d, "v": v, "reach_last": rl, "iterations": o.iters_total,
+           "warm_used": o.warm_used, "warm_fallback": o.warm_fallback}
     if history:
         out["q_hist"] = hist
+    if depth_history:
+        out["d_hist"] = dhist
+    if iter_history:
+        out["it_hist"] = ihist
     return out
+
+
+def mc_solve_warm(dt, qup, quc, qdp, ql, p_record, depthp, start, delta, k, tol=REF_TOL):
+    """One warm-started segment solve -> (q, depth, velocity, iterations, warm_state)."""
+    p = _params(np.asarray(p_record).reshape(1, -1) if np.asarray(p_record).dtype.names is None else p_record)
+    d, v, it, st = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+    t = _tol(tol)
+    q = oracle().oracle_mc_solve_warm(dt, qup, quc, qdp, ql, _ptr(p), depthp, C.byref(t), float(start), float(delta),
+                                      int(k), C.byref(d), C.byref(v), C.byref(it), C.byref(st))
+    return q, d.value, v.value, it.value, st.value
 
 
 def levels(up_ptr, up_idx, R):
