@@ -3,20 +3,33 @@
 
 Metric: segment-steps per second (segments x routed time steps / s) of FP64
 Muskingum-Cunge secant tree routing at secant tolerance rtol = 1e-8
-(atol = 1e-10), default workload c1: a 2.7M-segment, ~1.1M-reach random binary
-river tree (~2,400 levels), 144 steps of dt = 300 s, seeded synthetic
-parameters and lateral inflow (no dataset is available offline).
+(atol = 1e-10), batched + learned warm start against plain MC.
 
-One bench "step" = one whole 144-step routing run of the network (the state
-carries over from run to run), replayed from a captured CUDA graph with the
-lateral inflow (3.1 GB, larger than L2) resident in HBM. `e2e` is the same
-metric through the public C ABI with host buffers: troute_run (copies the
-step's lateral inflow from pinned host memory) plus troute_get_state (copies
-the routed discharge, depth, velocity and reach outflow back).
+Default workload c4w (the combined form): a 64-member ensemble over the
+2.7M-segment, ~1.1M-reach random binary river tree (~2,400 levels) -- lateral
+inflow x LogN(0, 0.3) and Manning's n x U(0.8, 1.2) per member -- routed in one
+persistent launch with the learned warm start, FP64 state. The MLP is trained
+in the same run, untimed, on (input, converged depth) pairs of an 18-step
+plain run of the single network (~49M pairs). One bench "step" = 8 routed
+time steps of all 64 members (1.4G segment-steps), replayed from a captured
+CUDA graph, the state carrying over. Beside it, in the same run, the plain
+single-basin routing of the same network (144 steps per graph launch) is
+timed: `plain_single_basin`, and `speedup_vs_plain` = value / that.
+
+Other workloads: c1 (plain single basin, 144 steps per bench step), c0, c2
+(256 uneven basins), c3 (warm start on a fresh-seed c1 network, trained on
+pairs of the seed-1001 network), c4 (the ensemble without warm start),
+tree:<segments>. Seeded synthetic parameters and lateral inflow (no dataset
+is available offline).
+
+`e2e` is the same metric through the public C ABI with host buffers:
+troute_run (copies the step's lateral inflow from pinned host memory) plus
+troute_get_state (copies the routed discharge, depth, velocity and reach
+outflow back).
 
 --impl reference times the reference's CPU algorithm (the oracle port of
-cpu_wavefront_fp64, all host threads, one routed time step of the same
-network per bench step).
+cpu_wavefront_fp64, all host threads, one routed time step of the network --
+of ensemble member 0 for c4/c4w -- per bench step).
 """
 from __future__ import annotations
 
@@ -49,7 +62,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1")
+    ap.add_argument("--workload", default="c4w")
     ap.add_argument("--n-ts", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -170,10 +183,12 @@ def profiled_traffic_per_seg_step():
     return None
 
 
-def workload(name: str, n_ts: int | None):
-    """Single networks ('c1', 'c0', 'tree:<segments>') or the batched forms:
-    'c2' (256 basins with LogU(500, 200,000) segments, 288 steps) and
-    'c4' (64 ensemble members of the c1 network, 288 steps)."""
+def workload(name: str, n_ts: int | None, all_members: bool = True):
+    """Single networks ('c1', 'c0', 'tree:<segments>', 'c3' = fresh-seed c1
+    with warm start) or the batched forms: 'c2' (256 basins with
+    LogU(500, 200,000) segments, 288 steps), 'c4' / 'c4w' (64 ensemble
+    members of the c1 network, without / with warm start; 8 steps per bench
+    step)."""
     from troute_gb300 import synth
 
     if name == "c2":
@@ -187,18 +202,25 @@ def workload(name: str, n_ts: int | None):
         w["rl0"] = np.concatenate([np.full(len(n["topo"]["reach_seg_start"]), synth.Q0) for n in nets])
         w["S"], w["R"] = S, len(w["rl0"])
         return w
-    if name == "c4":
+    if name in ("c4", "c4w"):
         M = 64
-        T = 288 if n_ts is None else n_ts
+        T = 8 if n_ts is None else n_ts
         w = synth.network("c1", n_ts=T)
         S = w["topo"]["n_segments"]
-        qf = np.empty((M, S))
-        nf = np.empty((M, S))
-        for m in range(M):
+        Mg = M if all_members else 1   # the CPU legs route member 0 only
+        qf = np.empty((Mg, S))
+        nf = np.empty((Mg, S))
+        for m in range(Mg):
             qf[m], nf[m] = synth.make_member(1004, m, S)
-        w.update(name=name, members=M, qfac=qf, nfac=nf)
+        w.update(name=name, members=M, qfac=qf, nfac=nf, warm=(name == "c4w"))
         w["S"], w["R"] = M * S, M * len(w["topo"]["reach_seg_start"])
+        w["q0_1"], w["d0_1"], w["rl0_1"] = w["q0"], w["d0"], w["rl0"]
         w["q0"], w["d0"], w["rl0"] = np.tile(w["q0"], M), np.tile(w["d0"], M), np.tile(w["rl0"], M)
+        return w
+    if name == "c3":
+        w = synth.network("c1", seed=2001, n_ts=n_ts)
+        w["name"], w["warm"] = "c3", True
+        w["S"], w["R"] = w["topo"]["n_segments"], len(w["topo"]["reach_seg_start"])
         return w
     w = synth.network(name, n_ts=n_ts)
     w["S"], w["R"] = w["topo"]["n_segments"], len(w["topo"]["reach_seg_start"])
@@ -216,26 +238,99 @@ def make_network(T, w, cfg):
 
 
 def describe(w) -> str:
+    ws = ", learned warm start" if w.get("warm") else ", plain secant start"
     if "batch" in w:
-        return f"batched: {len(w['batch'])} independent basins in one launch"
+        return f"batched: {len(w['batch'])} independent basins in one launch" + ws
     if "members" in w:
-        return f"batched: {w['members']}-member ensemble in one launch"
-    return "plain, single basin"
+        return f"batched: {w['members']}-member ensemble in one launch" + ws
+    return "single basin" + ws
+
+
+WARM_DELTA = 0.05   # relative half-width of the bracket around the learned depth
+WARM_K = 16         # secant passes before the plain fallback
+PAIR_STEPS = 18     # plain steps whose solves give the training pairs (~49M for c1)
+
+
+def train_and_plain(T, torch, dev, stream, plain_steps: int, plain_warmup: int) -> tuple:
+    """Untimed set-up of the warm-started workloads, on the seed-1001 c1
+    network: the training pairs of an 18-step plain run, the MLP trained on
+    them, then the plain single-basin routing timed (144 steps per graph
+    launch, the same method as the c1 workload)."""
+    from troute_gb300 import synth
+
+    w = synth.network("c1", n_ts=144)
+    S = w["topo"]["n_segments"]
+    ql = torch.from_numpy(np.ascontiguousarray(w["qlat"])).to(dev)
+    net = T.Network(w["topo"], w["params"], cfg=T.make_cfg(**TIGHT, record_pairs=1))
+    net.set_state(w["q0"], w["d0"], w["rl0"])
+    t0 = time.perf_counter()
+    net.run_device(ql.data_ptr(), PAIR_STEPS, stream.cuda_stream)
+    net.sync()
+    n = net.pairs()
+    pairs = torch.empty((n, 9), dtype=torch.float32, device=dev)
+    net.pairs(pairs.data_ptr(), n)
+    torch.cuda.synchronize(dev)
+    t_pairs = time.perf_counter() - t0
+    model = T.WarmModel(1001)
+    t0 = time.perf_counter()
+    loss = model.fit(pairs.data_ptr(), n, epochs=3, batch=8192, lr=2e-3, seed=1001)
+    t_fit = time.perf_counter() - t0
+    del pairs
+    # plain single-basin routing, graph-replayed 144-step runs
+    net.set_cfg(T.make_cfg(**TIGHT))
+    net.graph_capture(ql.data_ptr(), 144)
+    for _ in range(plain_warmup):
+        net.graph_launch(stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    net.sync()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(plain_steps):
+        net.graph_launch(stream.cuda_stream)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    st = net.sync()
+    ms = a.elapsed_time(b)
+    net.close()
+    del ql
+    torch.cuda.empty_cache()
+    plain = {"value": S * 144 * plain_steps / (ms / 1e3), "unit": UNIT,
+             "workload": f"c1: the same 2.7M-segment network alone, plain secant start, 144 steps per graph "
+                         f"launch, {plain_steps} timed launches after {plain_warmup}",
+             "iterations_per_solve": st["iterations"] / max(1, st["solves"]), "ms_per_run": ms / plain_steps}
+    info = {"pairs": int(n), "pair_steps": PAIR_STEPS, "pairs_s": round(t_pairs, 2), "epochs": 3, "batch": 8192,
+            "fit_s": round(t_fit, 2), "loss_per_epoch": [round(float(x), 5) for x in loss],
+            "delta": WARM_DELTA, "k": WARM_K, "trained_on": "c1 seed 1001, plain run from the initial state"}
+    return model, info, plain
+
+
+def single_network(w) -> tuple:
+    """(topo, params, qlat, q0, d0, rl0, label) of the network the CPU legs
+    route: the workload's network, or ensemble member 0 (its perturbed
+    Manning's n and lateral inflow) for the ensembles."""
+    if "members" in w:
+        p = w["params"].copy()
+        p["n_ch"] *= w["nfac"][0]
+        p["ncc"] *= w["nfac"][0]
+        return (w["topo"], p, w["qlat"] * w["qfac"][0][None, :], w["q0_1"], w["d0_1"], w["rl0_1"],
+                "ensemble member 0 of the")
+    return w["topo"], w["params"], w["qlat"], w["q0"], w["d0"], w["rl0"], "the"
 
 
 def cpu_baseline(w) -> dict:
     """The oracle port of cpu_wavefront_fp64, one core, one routed step of the
-    same network from its initial state."""
+    same network from its initial state (plain secant start, the reference's)."""
     from oracle import troute_oracle as O
 
     O.build(ref=False)
     tol = (TIGHT["rtol"], TIGHT["atol"], TIGHT["maxiter"], TIGHT["attempts"])
-    S = w["topo"]["n_segments"]
+    topo, params, qlat, q0, d0, rl0, label = single_network(w)
+    S = topo["n_segments"]
     t0 = time.perf_counter()
-    O.route_tree(w["topo"], w["params"], w["qlat"][:1], w["q0"], w["d0"], w["rl0"], tol=tol, threads=1)
+    O.route_tree(topo, params, qlat[:1], q0, d0, rl0, tol=tol, threads=1)
     dt = time.perf_counter() - t0
     return {"value": S / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"1 routed step of the {S}-segment network from its initial state, rtol 1e-8, "
+            "sample": f"1 routed step of {label} {S}-segment network from its initial state, rtol 1e-8, "
                       f"single thread ({dt:.1f} s)"}
 
 
@@ -246,18 +341,22 @@ def run_reference(args, dist: Dist):
     from oracle import troute_oracle as O
 
     O.build(ref=False)
-    w = workload(args.workload, args.n_ts)
-    S = w["topo"]["n_segments"]
+    w = workload(args.workload, args.n_ts, all_members=False)
+    if "topo" not in w:
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU arm routes single networks and ensemble "
+                                                            "members; run it with --workload c1 for c2"}))
+        return
+    topo, params, qlat, q, d, rl, label = single_network(w)
+    S = topo["n_segments"]
     nth = os.cpu_count() or 1
     tol = (TIGHT["rtol"], TIGHT["atol"], TIGHT["maxiter"], TIGHT["attempts"])
-    lp, lr = O.levels(w["topo"]["reach_up_ptr"], w["topo"]["reach_up_idx"], len(w["topo"]["reach_seg_start"]))
-    q, d, rl = w["q0"], w["d0"], w["rl0"]
-    T = w["qlat"].shape[0]
+    lp, lr = O.levels(topo["reach_up_ptr"], topo["reach_up_idx"], len(topo["reach_seg_start"]))
+    T = qlat.shape[0]
     times = []
     for k in range(args.warmup + args.steps):
         t = k % T
         t0 = time.perf_counter()
-        o = O.route_tree(w["topo"], w["params"], w["qlat"][t:t + 1], q, d, rl, tol=tol, threads=nth,
+        o = O.route_tree(topo, params, qlat[t:t + 1], q, d, rl, tol=tol, threads=nth,
                          level_ptr=lp, level_reach=lr)
         el = time.perf_counter() - t0
         q, d, rl = o["q"], o["d"], o["reach_last"]
@@ -269,11 +368,11 @@ def run_reference(args, dist: Dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generator)",
-            "config": {"workload": f"{args.workload}: FP64 MC secant tree routing, {S} segments, "
-                                   f"{len(w['topo']['reach_seg_start'])} reaches, rtol 1e-8; one routed step "
-                                   f"per bench step", "segments": S},
+            "config": {"workload": f"{args.workload}: FP64 MC secant tree routing of {label} {S}-segment "
+                                   f"network, {len(topo['reach_seg_start'])} reaches, rtol 1e-8, plain secant "
+                                   f"start (the reference's); one routed step per bench step", "segments": S},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
-                             "sample": f"1 routed time step of the {S}-segment network per bench step, "
+                             "sample": f"1 routed time step of {label} {S}-segment network per bench step, "
                                        f"{nth} threads (level-parallel oracle port of cpu_wavefront_fp64)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -291,13 +390,18 @@ def run_ours(args, dist: Dist):
     S, R = w["S"], w["R"]
     n_ts = w["qlat"].shape[0]
     cols = w["qlat"].shape[1]
-    cfg = T.make_cfg(**TIGHT)
+    stream = torch.cuda.Stream(dev)   # a real stream: 0 would mean "the handle's own stream"
+    model = warm_info = plain = None
+    if w.get("warm"):
+        model, warm_info, plain = train_and_plain(T, torch, dev, stream, plain_steps=2, plain_warmup=1)
+    cfg = T.make_cfg(**TIGHT, warm_start=1 if model else 0, warm_k=WARM_K)
     net = make_network(T, w, cfg)
+    if model:
+        net.set_warm_start(model, WARM_DELTA)
     net.set_state(w["q0"], w["d0"], w["rl0"])
     qlat_host = torch.empty((n_ts, cols), dtype=torch.float64, pin_memory=True)
     qlat_host.numpy()[:] = w["qlat"]
     qlat_dev = qlat_host.to(dev, non_blocking=False)
-    stream = torch.cuda.Stream(dev)   # a real stream: 0 would mean "the handle's own stream"
     levels = net.n_levels
     net.graph_capture(qlat_dev.data_ptr(), n_ts)
     for _ in range(args.warmup):
@@ -350,25 +454,29 @@ def run_ours(args, dist: Dist):
         qh = qlat_host.numpy()
         net.close()
         net2 = make_network(T, w, cfg)
+        if model:
+            net2.set_warm_start(model, WARM_DELTA)
         net2.set_state(w["q0"], w["d0"], w["rl0"])
+        e2e_steps = min(args.steps, 2) if "members" in w else args.steps
         for _ in range(1):
             net2.run(qh)
             net2.get_state()
         torch.cuda.synchronize(dev)
         dist.barrier()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(e2e_steps):
             net2.run(qh)
             net2.get_state()
         t1 = time.perf_counter()
         dist.barrier()
         e2e_s = dist.max(t1 - t0)
-        e2e = {"value": seg_steps * args.steps * dist.world / e2e_s, "unit": UNIT,
-               "h2d_bytes_per_step": int(qh.nbytes), "d2h_bytes_per_step": int((3 * S + R) * 8)}
+        e2e = {"value": seg_steps * e2e_steps * dist.world / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(qh.nbytes), "d2h_bytes_per_step": int((3 * S + R) * 8),
+               "steps": e2e_steps}
         net2.close()
 
     cpu = None
-    if dist.rank == 0 and not args.no_cpu_baseline and "topo" in w and "members" not in w:
+    if dist.rank == 0 and not args.no_cpu_baseline and "topo" in w:
         cpu = cpu_baseline(w)
     it = stats["iterations"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -378,12 +486,18 @@ def run_ours(args, dist: Dist):
                                    f"{S} segments, {R} reaches, {levels} levels, {n_ts} steps of "
                                    f"{w['dt']:.0f} s per bench step, rtol 1e-8 atol 1e-10",
                        "segments": S, "reaches": R, "levels": levels, "timesteps_per_step": n_ts,
-                       "l2": "inputs larger than L2 (lateral inflow 3.1 GB read per step)",
+                       "l2": f"inputs larger than L2 (129 MB): lateral inflow {w['qlat'].nbytes / 1e9:.2f} GB and "
+                             f"segment parameters {S * 96 / 1e9:.2f} GB read per bench step",
                        "parallelism": "replicas" if dist.world > 1 else "single GPU"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 4 * args.steps,
             "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
-                       "early_exits": stats["early_exits"]}}
+                       "early_exits": stats["early_exits"], "warm_used": stats["warm_used"],
+                       "warm_fallback_rate": stats["warm_fallback"] / max(1, stats["warm_used"])}}
+    if model:
+        line["warm_model"] = warm_info
+        line["plain_single_basin"] = plain
+        line["speedup_vs_plain"] = value / plain["value"]
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 

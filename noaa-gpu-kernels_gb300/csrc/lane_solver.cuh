@@ -36,7 +36,6 @@ struct Lane {
     double qup_head, quc_head, q_up_old, q_up_new, q_last;
     // current segment
     long long s;
-    SegP p;
     double qup, quc, qdp, ql;
     double h, h_0, Qj_0, qdc;
     double dpp;            // previous depth (clamped at 0): the plain bracket's centre
@@ -71,10 +70,9 @@ __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const 
         const double dpp = __ldcg(net.d + L.s);
         L.ql = __ldg(qlat_row + __ldg(net.qcol + L.s));
         if (net.qscale) L.ql *= __ldg(net.qscale + L.s);
-        L.p = load_seg(net, L.s);
+        const SegP p = load_seg(net, L.s);
         L.qup = (L.i == 0) ? L.qup_head : L.q_up_old;
         L.quc = (L.i == 0) ? L.quc_head : L.q_up_new;
-        const SegP& p = L.p;
         if (p.n_ch <= 0.0 || p.s0 <= 0.0 || p.z <= 0.0 || p.bw <= 0.0 ||
             (L.ql <= 0.0 && L.qup <= 0.0 && L.quc <= 0.0 && L.qdp <= 0.0)) {
             __stcg(net.q + L.s, 0.0);
@@ -109,7 +107,9 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
     const Tol& tol = run.tol;
     const double dt = run.dt;
     if (L.mode == L_SOLVE && L.warm != W_PENDING) {
-        const SegP& p = L.p;
+        // the segment's parameters are re-read (L1) every pass rather than held
+        // in registers across the kernel's scheduling code
+        const SegP p = load_seg(net, L.s);
         const double x = L.need0 ? L.h_0 : L.h;
         const double twl = p.bw + 2.0 * p.z * x;
         double above = fmax(x - p.bfd, 0.0);

@@ -103,8 +103,8 @@ __device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base,
 // (W_PENDING): one tensor-core MLP evaluation for the whole warp, then the
 // bracket [p (1 - delta), p (1 + delta)] around the prediction p. A prediction
 // that is not a positive finite depth below 1e4 m leaves the plain bracket.
-__device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const WarmDev& m, const RunDev& run,
-                                                   long long n_seg_int, LocalStats& ls)
+__device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const WarmDev& m, const NetDev& net,
+                                                   const RunDev& run, LocalStats& ls)
 {
     const bool pend = (L.mode == L_SOLVE && L.warm == W_PENDING);
     if (!__any_sync(0xffffffffu, pend)) return;
@@ -114,14 +114,15 @@ __device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const W
         f[1] = warm_feature(L.quc, true, m.mu[1], m.sd[1]);
         f[2] = warm_feature(L.qdp, true, m.mu[2], m.sd[2]);
         f[3] = warm_feature(L.ql, true, m.mu[3], m.sd[3]);
-        f[4] = warm_feature(L.p.dx, false, m.mu[4], m.sd[4]);
-        f[5] = warm_feature(L.p.s0, false, m.mu[5], m.sd[5]);
-        f[6] = warm_feature(L.p.n_ch, false, m.mu[6], m.sd[6]);
-        f[7] = warm_feature(L.p.bw, false, m.mu[7], m.sd[7]);
+        const double2 p0 = __ldg(net.prm[0] + L.s), p1 = __ldg(net.prm[1] + L.s), p2 = __ldg(net.prm[2] + L.s);
+        f[4] = warm_feature(p0.x, false, m.mu[4], m.sd[4]);   // dx
+        f[5] = warm_feature(p2.y, false, m.mu[5], m.sd[5]);   // s0
+        f[6] = warm_feature(p1.y, false, m.mu[6], m.sd[6]);   // n
+        f[7] = warm_feature(p0.y, false, m.mu[7], m.sd[7]);   // bw
     } else {
         for (int k = 0; k < kWIn; ++k) f[k] = 0.0f;
     }
-    const float y = warm_mlp_warp(s, f, m.b3);
+    const float y = warm_mlp_warp(s, f, pend, m.b3);
     if (pend) {
         const double pr = (double)expf(y * m.sd_y + m.mu_y);
         if (pr > 0.0 && pr < 1.0e4) {
@@ -129,15 +130,25 @@ __device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const W
             L.h_0 = pr * (1.0 - run.warm_delta);
             L.warm = W_ACTIVE;
             ls.warm_used++;
-            if (run.start_hist) __stcg(run.start_hist + (size_t)L.tau * (size_t)n_seg_int + L.s, pr);
+            if (run.start_hist) __stcg(run.start_hist + (size_t)L.tau * (size_t)net.n_seg_int + L.s, pr);
         } else {
             L.warm = W_PLAIN;
         }
     }
 }
 
+// Resident blocks per SM the register allocation is sized for (plain and
+// warm-started kernels).
+#ifndef TROUTE_DF_MINB
+#define TROUTE_DF_MINB 1
+#endif
+#ifndef TROUTE_DFW_MINB
+#define TROUTE_DFW_MINB 3
+#endif
+
 template <bool WARM>
-__global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df, WarmDev wm)
+__global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
+    route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df, WarmDev wm)
 {
     __shared__ unsigned int hist_s[16];
     extern __shared__ __align__(16) unsigned char dyn_smem[];
@@ -255,7 +266,7 @@ __global__ void __launch_bounds__(128) route_dataflow_kernel(NetDev net, RunDev 
         }
 
         // ---- learned starting depths for solves that just began ----
-        if constexpr (WARM) warm_predict_lanes(L, wsm, wm, run, net.n_seg_int, ls);
+        if constexpr (WARM) warm_predict_lanes(L, wsm, wm, net, run, ls);
 
         // ---- one depth evaluation per solving lane ----
         if (__any_sync(kFullMask, L.mode >= L_SOLVE)) lane_pass(L, net, run, ls, hist_s);

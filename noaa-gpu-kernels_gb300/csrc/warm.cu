@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(128) warm_predict_kernel(WarmDev m, const floa
         const double v = (i < n) ? (double)raw[(size_t)i * kWIn + k] : 1.0;
         f[k] = warm_feature(v, k < 4, m.mu[k], m.sd[k]);
     }
-    const float yh = warm_mlp_warp(s, f, m.b3);
+    const float yh = warm_mlp_warp(s, f, i < n, m.b3);
     if (i < n) depth[i] = (double)__expf(yh * m.sd_y + m.mu_y);
 }
 

@@ -70,7 +70,17 @@ __device__ __forceinline__ unsigned int pack_bf16(float lo, float hi)
     return *reinterpret_cast<const unsigned int*>(&v);
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU through the hardware tanh approximation: z sigmoid(z) = z (1 + tanh(z/2)) / 2
+// (the training kernels use the exact form; the difference is far below the
+// BF16 rounding of the activations).
+__device__ __forceinline__ float tanh_approx(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float silu(float z) { return 0.5f * z * (1.0f + tanh_approx(0.5f * z)); }
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
 {
@@ -83,74 +93,98 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], 
 
 __device__ __forceinline__ unsigned ld_pair(const __nv_bfloat16* p) { return *reinterpret_cast<const unsigned*>(p); }
 
-// Evaluates the MLP for the 32 rows of a warp (row = lane). Every lane of the
-// warp must call it (it uses warp-synchronous MMA); `feat` is the lane's 8
-// normalised features (ignored for lanes whose prediction is not used).
-// Returns the prediction of the lane's own row in normalised units.
-static __device__ __noinline__ float warm_mlp_warp(WarmSmem& s, const float (&feat)[kWIn], float b3)
+// One 16-row tile of the MLP (rows mt*16 .. mt*16+15 of the warp's staging
+// area). Returns the C fragment of the output column: rows g (o0) and g + 8
+// (o2) on the lanes with t == 0.
+__device__ __forceinline__ void warm_mlp_tile(const WarmSmem& s, int w, int mt, int g, int t, float b3, float& o0,
+                                              float& o2)
+{
+    // ---- layer 1: [16 x 16(8)] x [16 x 64] ----
+    unsigned a[4];
+    a[0] = s.xin[w][mt * 16 + g][t];
+    a[1] = s.xin[w][mt * 16 + g + 8][t];
+    a[2] = 0u;
+    a[3] = 0u;
+    unsigned a2[4][4];  // SiLU(h1) as the A fragments of layer 2 (C -> A in registers)
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+        float h[2][4];
+#pragma unroll
+        for (int jj = 0; jj < 2; ++jj) {
+            const int j = 2 * kk + jj, n = 8 * j + 2 * t;
+            h[jj][0] = s.b1[n];
+            h[jj][1] = s.b1[n + 1];
+            h[jj][2] = s.b1[n];
+            h[jj][3] = s.b1[n + 1];
+            mma_bf16(h[jj], a, ld_pair(&s.w1t[8 * j + g][2 * t]), ld_pair(&s.w1t[8 * j + g][8 + 2 * t]));
+        }
+        a2[kk][0] = pack_bf16(silu(h[0][0]), silu(h[0][1]));
+        a2[kk][1] = pack_bf16(silu(h[0][2]), silu(h[0][3]));
+        a2[kk][2] = pack_bf16(silu(h[1][0]), silu(h[1][1]));
+        a2[kk][3] = pack_bf16(silu(h[1][2]), silu(h[1][3]));
+    }
+    // ---- layers 2 and 3, one 16-column chunk of the hidden layer at a time ----
+    float o[4] = {b3, b3, b3, b3};
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+        float h[2][4];
+#pragma unroll
+        for (int jj = 0; jj < 2; ++jj) {
+            const int j = 2 * kk + jj, n = 8 * j + 2 * t;
+            h[jj][0] = s.b2[n];
+            h[jj][1] = s.b2[n + 1];
+            h[jj][2] = s.b2[n];
+            h[jj][3] = s.b2[n + 1];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                mma_bf16(h[jj], a2[q], ld_pair(&s.w2t[8 * j + g][16 * q + 2 * t]),
+                         ld_pair(&s.w2t[8 * j + g][16 * q + 8 + 2 * t]));
+        }
+        unsigned a3[4];
+        a3[0] = pack_bf16(silu(h[0][0]), silu(h[0][1]));
+        a3[1] = pack_bf16(silu(h[0][2]), silu(h[0][3]));
+        a3[2] = pack_bf16(silu(h[1][0]), silu(h[1][1]));
+        a3[3] = pack_bf16(silu(h[1][2]), silu(h[1][3]));
+        mma_bf16(o, a3, ld_pair(&s.w3t[g][16 * kk + 2 * t]), ld_pair(&s.w3t[g][16 * kk + 8 + 2 * t]));
+    }
+    o0 = o[0];
+    o2 = o[2];
+}
+
+// Evaluates the MLP for the lanes of a warp that ask for it (`want`). Every
+// lane of the warp must call it (warp-synchronous MMA). The asking lanes'
+// feature rows are packed into the first rows of the warp's staging area, so
+// up to 16 requests cost one 16-row tile and more cost two. Each output row
+// depends on its own input row only. Returns the prediction (normalised
+// units) on the asking lanes.
+#ifdef TROUTE_MLP_INLINE
+#define TR_MLP_ATTR __forceinline__
+#else
+#define TR_MLP_ATTR __noinline__
+#endif
+static __device__ TR_MLP_ATTR float warm_mlp_warp(WarmSmem& s, const float (&feat)[kWIn], bool want, float b3)
 {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
-    unsigned int* xin = s.xin[w][lane];
-    xin[0] = pack_bf16(feat[0], feat[1]);
-    xin[1] = pack_bf16(feat[2], feat[3]);
-    xin[2] = pack_bf16(feat[4], feat[5]);
-    xin[3] = pack_bf16(feat[6], feat[7]);
-    __syncwarp();
-    float out_rows[2][2];  // [m-tile][half]: prediction of rows g, g+8 (valid on lanes with t == 0)
-    for (int mt = 0; mt < 2; ++mt) {
-        // ---- layer 1: [16 x 16(8)] x [16 x 64] ----
-        unsigned a[4];
-        a[0] = s.xin[w][mt * 16 + g][t];
-        a[1] = s.xin[w][mt * 16 + g + 8][t];
-        a[2] = 0u;
-        a[3] = 0u;
-        float h1[8][4];
-        for (int j = 0; j < 8; ++j) {
-            const int n = 8 * j + 2 * t;
-            h1[j][0] = s.b1[n];
-            h1[j][1] = s.b1[n + 1];
-            h1[j][2] = s.b1[n];
-            h1[j][3] = s.b1[n + 1];
-            mma_bf16(h1[j], a, ld_pair(&s.w1t[8 * j + g][2 * t]), ld_pair(&s.w1t[8 * j + g][8 + 2 * t]));
-        }
-        // ---- layer 2: SiLU(h1) [16 x 64] x [64 x 64]; C fragments become A fragments ----
-        unsigned a2[4][4];
-        for (int kk = 0; kk < 4; ++kk) {
-            a2[kk][0] = pack_bf16(silu(h1[2 * kk][0]), silu(h1[2 * kk][1]));
-            a2[kk][1] = pack_bf16(silu(h1[2 * kk][2]), silu(h1[2 * kk][3]));
-            a2[kk][2] = pack_bf16(silu(h1[2 * kk + 1][0]), silu(h1[2 * kk + 1][1]));
-            a2[kk][3] = pack_bf16(silu(h1[2 * kk + 1][2]), silu(h1[2 * kk + 1][3]));
-        }
-        float h2[8][4];
-        for (int j = 0; j < 8; ++j) {
-            const int n = 8 * j + 2 * t;
-            h2[j][0] = s.b2[n];
-            h2[j][1] = s.b2[n + 1];
-            h2[j][2] = s.b2[n];
-            h2[j][3] = s.b2[n + 1];
-            for (int kk = 0; kk < 4; ++kk)
-                mma_bf16(h2[j], a2[kk], ld_pair(&s.w2t[8 * j + g][16 * kk + 2 * t]),
-                         ld_pair(&s.w2t[8 * j + g][16 * kk + 8 + 2 * t]));
-        }
-        // ---- layer 3: SiLU(h2) [16 x 64] x [64 x 8(1)] ----
-        float o[4] = {b3, b3, b3, b3};
-        for (int kk = 0; kk < 4; ++kk) {
-            unsigned a3[4];
-            a3[0] = pack_bf16(silu(h2[2 * kk][0]), silu(h2[2 * kk][1]));
-            a3[1] = pack_bf16(silu(h2[2 * kk][2]), silu(h2[2 * kk][3]));
-            a3[2] = pack_bf16(silu(h2[2 * kk + 1][0]), silu(h2[2 * kk + 1][1]));
-            a3[3] = pack_bf16(silu(h2[2 * kk + 1][2]), silu(h2[2 * kk + 1][3]));
-            mma_bf16(o, a3, ld_pair(&s.w3t[g][16 * kk + 2 * t]), ld_pair(&s.w3t[g][16 * kk + 8 + 2 * t]));
-        }
-        out_rows[mt][0] = o[0];  // row g, column 2t (column 0 on t == 0)
-        out_rows[mt][1] = o[2];  // row g + 8
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    const int rank = __popc(mask & ((1u << lane) - 1u));
+    if (want) {
+        unsigned int* xin = s.xin[w][rank];
+        xin[0] = pack_bf16(feat[0], feat[1]);
+        xin[1] = pack_bf16(feat[2], feat[3]);
+        xin[2] = pack_bf16(feat[4], feat[5]);
+        xin[3] = pack_bf16(feat[6], feat[7]);
     }
-    // row r = lane: m-tile r/16, row-in-tile rr = r%16 -> held by lane (rr%8)*4, half rr/8
-    const int rr = lane & 15, src = (rr & 7) * 4, half = rr >> 3, mt = lane >> 4;
-    const float v00 = __shfl_sync(0xffffffffu, out_rows[0][0], src);
-    const float v01 = __shfl_sync(0xffffffffu, out_rows[0][1], src);
-    const float v10 = __shfl_sync(0xffffffffu, out_rows[1][0], src);
-    const float v11 = __shfl_sync(0xffffffffu, out_rows[1][1], src);
+    __syncwarp();
+    const int n_tiles = __popc(mask) > 16 ? 2 : 1;
+    float r[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+    warm_mlp_tile(s, w, 0, g, t, b3, r[0][0], r[0][1]);
+    if (n_tiles == 2) warm_mlp_tile(s, w, 1, g, t, b3, r[1][0], r[1][1]);
+    // row `rank`: tile rank/16, row-in-tile rr = rank%16, held by lane (rr%8)*4, half rr/8
+    const int rr = rank & 15, src = (rr & 7) * 4, half = rr >> 3, mt = rank >> 4;
+    const float v00 = __shfl_sync(0xffffffffu, r[0][0], src);
+    const float v01 = __shfl_sync(0xffffffffu, r[0][1], src);
+    const float v10 = __shfl_sync(0xffffffffu, r[1][0], src);
+    const float v11 = __shfl_sync(0xffffffffu, r[1][1], src);
     __syncwarp();
     return mt == 0 ? (half ? v01 : v00) : (half ? v11 : v10);
 }
