@@ -294,6 +294,28 @@ int troute_levels(int n_reaches, const int* reach_up_ptr, const int* reach_up_id
 /* Checks a topology; returns TROUTE_OK or TROUTE_ETOPO with a message. */
 int troute_validate(const troute_topo* topo);
 
+/* ---- on-disk network format ------------------------------------------- */
+/* The reference's topo.bin / params.bin / forcings.bin directory format
+ * (water-prediction/t-route/wavefront/gen_network.py:292-337, read by
+ * wavefront_mc.cu:597-632 load_topo and :655-672). All arrays are owned by
+ * the struct; troute_read_network allocates, troute_free_network releases.
+ * params are float32 as the reference writes them; qlat is [n_ts][n_segments];
+ * qup0 is the per-reach outflow of the step before the first (reach_last0). */
+typedef struct troute_netfile {
+    int n_reaches, n_segments, n_levels, max_upstream, n_ts;
+    int *reach_seg_start, *reach_seg_len, *reach_level, *reach_n_up;
+    int *reach_up_ptr, *reach_up_idx;   /* [n_reaches + 1], [nnz] */
+    int *level_ptr, *level_reach;       /* [n_levels + 1], [n_reaches] */
+    troute_chparams_f32* params;        /* [n_segments] */
+    float *qlat, *qup0, *qdp0, *dp0;
+} troute_netfile;
+/* Reads and checks the three files (short, long or inconsistent files give
+ * TROUTE_EIO / TROUTE_ETOPO; the reference's reader exits or reads short). */
+int troute_read_network(const char* dir, troute_netfile** net);
+void troute_free_network(troute_netfile* net);
+/* Writes the three files (byte-compatible with the reference's writer). */
+int troute_write_network(const char* dir, const troute_netfile* net);
+
 /* ---- synthetic inputs (seeded, platform-independent) ------------------ */
 /* Uniform random binary river tree (Remy's algorithm) with n_leaves
  * headwaters -> 2*n_leaves-1 reaches, n_segments segments of 1..max_len per

@@ -155,6 +155,9 @@ _SIGS = {
     "troute_set_warm_start": ([_P, _P, _D], _I),
     "troute_get_pairs": ([_P, _P, C.c_longlong, _P], _I),
     "troute_get_start_history": ([_P, _P, _I], _I),
+    "troute_read_network": ([C.c_char_p, _P], _I),
+    "troute_free_network": ([_P], None),
+    "troute_write_network": ([C.c_char_p, _P], _I),
     "troute_debug_timeout_probe": ([C.c_longlong], _I),
     "troute_debug_pow": ([_P, _I, _P], _I),
     "troute_levels": ([_I, _P, _P, _P, _P, _P, _P], _I),
@@ -479,6 +482,68 @@ class Network:
     def restore(self, blob: bytes):
         buf = C.create_string_buffer(blob, len(blob))
         _check(lib().troute_restore(self._h, buf, len(blob)))
+
+
+class NetFile(C.Structure):
+    _fields_ = [("n_reaches", C.c_int), ("n_segments", C.c_int), ("n_levels", C.c_int), ("max_upstream", C.c_int),
+                ("n_ts", C.c_int)] + [(k, C.c_void_p) for k in (
+                    "reach_seg_start", "reach_seg_len", "reach_level", "reach_n_up", "reach_up_ptr", "reach_up_idx",
+                    "level_ptr", "level_reach", "params", "qlat", "qup0", "qdp0", "dp0")]
+
+
+_NET_INT = ("reach_seg_start", "reach_seg_len", "reach_level", "reach_n_up", "reach_up_ptr", "reach_up_idx",
+            "level_ptr", "level_reach")
+
+
+def read_network(path: str) -> dict:
+    """Reads a topo.bin / params.bin / forcings.bin directory (the reference's
+    format) -> dict of numpy arrays (params as float32 ChParams records)."""
+    ptr = C.POINTER(NetFile)()
+    _check(lib().troute_read_network(os.fsencode(path), C.byref(ptr)))
+    try:
+        n = ptr.contents
+        R, S, L, T = n.n_reaches, n.n_segments, n.n_levels, n.n_ts
+        nnz = int(np.ctypeslib.as_array(C.cast(n.reach_up_ptr, C.POINTER(C.c_int)), (R + 1,))[R])
+        sizes = {"reach_seg_start": R, "reach_seg_len": R, "reach_level": R, "reach_n_up": R,
+                 "reach_up_ptr": R + 1, "reach_up_idx": nnz, "level_ptr": L + 1, "level_reach": R}
+        out = {"n_reaches": R, "n_segments": S, "n_levels": L, "max_upstream": n.max_upstream, "n_ts": T}
+        for k, m in sizes.items():
+            a = getattr(n, k)
+            out[k] = np.ctypeslib.as_array(C.cast(a, C.POINTER(C.c_int)), (m,)).copy() if m else np.zeros(0, np.int32)
+        pf = np.ctypeslib.as_array(C.cast(n.params, C.POINTER(C.c_float)), (S * 8,)).copy() if S else np.zeros(0, np.float32)
+        out["params"] = pf.view(CHPARAMS_F32_DTYPE).reshape(-1)
+        f = lambda a, m: (np.ctypeslib.as_array(C.cast(a, C.POINTER(C.c_float)), (m,)).copy() if m
+                          else np.zeros(0, np.float32))
+        out["qlat"] = f(n.qlat, T * S).reshape(T, S)
+        out["qup0"], out["qdp0"], out["dp0"] = f(n.qup0, R), f(n.qdp0, S), f(n.dp0, S)
+        return out
+    finally:
+        lib().troute_free_network(ptr)
+
+
+def write_network(path: str, net: dict):
+    """Writes a dict as returned by read_network as the reference's three files."""
+    keep = {}
+
+    def arr(k, dt):
+        a = np.ascontiguousarray(net[k], dt)
+        keep[k] = a
+        return a.ctypes.data_as(C.c_void_p)
+
+    n = NetFile()
+    n.n_reaches, n.n_segments, n.n_levels = int(net["n_reaches"]), int(net["n_segments"]), int(net["n_levels"])
+    n.max_upstream, n.n_ts = int(net["max_upstream"]), int(net["qlat"].shape[0])
+    for k in _NET_INT:
+        setattr(n, k, arr(k, np.int32))
+    p = np.ascontiguousarray(net["params"])
+    if p.dtype != CHPARAMS_F32_DTYPE:
+        p = np.ascontiguousarray(np.asarray(p, np.float32).reshape(-1, 8)).view(CHPARAMS_F32_DTYPE).reshape(-1)
+    keep["params"] = p
+    n.params = p.ctypes.data_as(C.c_void_p)
+    for k in ("qlat", "qup0", "qdp0", "dp0"):
+        setattr(n, k, arr(k, np.float32))
+    os.makedirs(path, exist_ok=True)
+    _check(lib().troute_write_network(os.fsencode(path), C.byref(n)))
 
 
 WARM_NPARAMS = 4801
