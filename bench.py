@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--n-ts", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--warm", action="store_true",
+                    help="learned warm start on a single-network workload (trained on its own plain-run pairs)")
     return ap.parse_args()
 
 
@@ -202,17 +204,24 @@ def workload(name: str, n_ts: int | None, all_members: bool = True):
         w["rl0"] = np.concatenate([np.full(len(n["topo"]["reach_seg_start"]), synth.Q0) for n in nets])
         w["S"], w["R"] = S, len(w["rl0"])
         return w
-    if name in ("c4", "c4w"):
-        M = 64
+    if name in ("c4", "c4w") or name.startswith("ens:"):
+        # ens:<members>:<segments>[:w] -- a smaller ensemble of a tree:<segments>
+        # network (profiling cases), ':w' with the warm start
+        if name.startswith("ens:"):
+            parts = name.split(":")
+            M, base_net = int(parts[1]), f"tree:{int(parts[2])}"
+        else:
+            M, base_net = 64, "c1"
         T = 8 if n_ts is None else n_ts
-        w = synth.network("c1", n_ts=T)
+        w = synth.network(base_net, n_ts=T)
+        w["base"] = base_net
         S = w["topo"]["n_segments"]
         Mg = M if all_members else 1   # the CPU legs route member 0 only
         qf = np.empty((Mg, S))
         nf = np.empty((Mg, S))
         for m in range(Mg):
             qf[m], nf[m] = synth.make_member(1004, m, S)
-        w.update(name=name, members=M, qfac=qf, nfac=nf, warm=(name == "c4w"))
+        w.update(name=name, members=M, qfac=qf, nfac=nf, warm=(name == "c4w" or name.endswith(":w")))
         w["S"], w["R"] = M * S, M * len(w["topo"]["reach_seg_start"])
         w["q0_1"], w["d0_1"], w["rl0_1"] = w["q0"], w["d0"], w["rl0"]
         w["q0"], w["d0"], w["rl0"] = np.tile(w["q0"], M), np.tile(w["d0"], M), np.tile(w["rl0"], M)
@@ -251,14 +260,15 @@ WARM_K = 16         # secant passes before the plain fallback
 PAIR_STEPS = 18     # plain steps whose solves give the training pairs (~49M for c1)
 
 
-def train_and_plain(T, torch, dev, stream, plain_steps: int, plain_warmup: int) -> tuple:
-    """Untimed set-up of the warm-started workloads, on the seed-1001 c1
-    network: the training pairs of an 18-step plain run, the MLP trained on
-    them, then the plain single-basin routing timed (144 steps per graph
-    launch, the same method as the c1 workload)."""
+def train_and_plain(T, torch, dev, stream, plain_steps: int, plain_warmup: int, base: str = "c1") -> tuple:
+    """Untimed set-up of the warm-started workloads, on the base network (the
+    seed-1001 c1 network for c3/c4w, else the workload's own network): the
+    training pairs of an 18-step plain run, the MLP trained on them, then the
+    plain single-basin routing timed (144 steps per graph launch, the same
+    method as the c1 workload)."""
     from troute_gb300 import synth
 
-    w = synth.network("c1", n_ts=144)
+    w = synth.network(base, n_ts=144)
     S = w["topo"]["n_segments"]
     ql = torch.from_numpy(np.ascontiguousarray(w["qlat"])).to(dev)
     net = T.Network(w["topo"], w["params"], cfg=T.make_cfg(**TIGHT, record_pairs=1))
@@ -295,12 +305,12 @@ def train_and_plain(T, torch, dev, stream, plain_steps: int, plain_warmup: int) 
     del ql
     torch.cuda.empty_cache()
     plain = {"value": S * 144 * plain_steps / (ms / 1e3), "unit": UNIT,
-             "workload": f"c1: the same 2.7M-segment network alone, plain secant start, 144 steps per graph "
+             "workload": f"{base}: the {S}-segment network alone, plain secant start, 144 steps per graph "
                          f"launch, {plain_steps} timed launches after {plain_warmup}",
              "iterations_per_solve": st["iterations"] / max(1, st["solves"]), "ms_per_run": ms / plain_steps}
     info = {"pairs": int(n), "pair_steps": PAIR_STEPS, "pairs_s": round(t_pairs, 2), "epochs": 3, "batch": 8192,
             "fit_s": round(t_fit, 2), "loss_per_epoch": [round(float(x), 5) for x in loss],
-            "delta": WARM_DELTA, "k": WARM_K, "trained_on": "c1 seed 1001, plain run from the initial state"}
+            "delta": WARM_DELTA, "k": WARM_K, "trained_on": f"{base} (seed {w['seed']}), plain run from the initial state"}
     return model, info, plain
 
 
@@ -392,8 +402,11 @@ def run_ours(args, dist: Dist):
     cols = w["qlat"].shape[1]
     stream = torch.cuda.Stream(dev)   # a real stream: 0 would mean "the handle's own stream"
     model = warm_info = plain = None
+    if args.warm and "topo" in w and "members" not in w:
+        w["warm"] = True
     if w.get("warm"):
-        model, warm_info, plain = train_and_plain(T, torch, dev, stream, plain_steps=2, plain_warmup=1)
+        base = w.get("base", "c1") if w["name"] in ("c3", "c4w") or "members" in w else w["name"]
+        model, warm_info, plain = train_and_plain(T, torch, dev, stream, plain_steps=2, plain_warmup=1, base=base)
     cfg = T.make_cfg(**TIGHT, warm_start=1 if model else 0, warm_k=WARM_K)
     net = make_network(T, w, cfg)
     if model:
@@ -403,6 +416,14 @@ def run_ours(args, dist: Dist):
     qlat_host.numpy()[:] = w["qlat"]
     qlat_dev = qlat_host.to(dev, non_blocking=False)
     levels = net.n_levels
+    tune = None
+    if "batch" in w or "members" in w:
+        # the batched forms pick their launch shape with the autotuner (a trial of
+        # half a bench step per candidate, from the same state; untimed)
+        t0 = time.perf_counter()
+        tune = net.autotune(qlat_dev.data_ptr(), max(1, n_ts // 2), repeats=1, all_mappings=not model)
+        tune["tune_s"] = round(time.perf_counter() - t0, 2)
+        tune["trial_steps"] = max(1, n_ts // 2)
     net.graph_capture(qlat_dev.data_ptr(), n_ts)
     for _ in range(args.warmup):
         net.graph_launch(stream.cuda_stream)
@@ -457,6 +478,10 @@ def run_ours(args, dist: Dist):
         if model:
             net2.set_warm_start(model, WARM_DELTA)
         net2.set_state(w["q0"], w["d0"], w["rl0"])
+        if tune:
+            net2.set_cfg(T.make_cfg(**TIGHT, warm_start=1 if model else 0, warm_k=WARM_K, mapping=tune["mapping"],
+                                    blocks_per_sm=tune["blocks_per_sm"], schedule_flags=tune["schedule_flags"],
+                                    threads_per_block=tune["threads_per_block"] if tune["mapping"] == 1 else 0))
         e2e_steps = min(args.steps, 2) if "members" in w else args.steps
         for _ in range(1):
             net2.run(qh)
@@ -494,6 +519,8 @@ def run_ours(args, dist: Dist):
             "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
                        "early_exits": stats["early_exits"], "warm_used": stats["warm_used"],
                        "warm_fallback_rate": stats["warm_fallback"] / max(1, stats["warm_used"])}}
+    if tune:
+        line["autotune"] = tune
     if model:
         line["warm_model"] = warm_info
         line["plain_single_basin"] = plain

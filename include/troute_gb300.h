@@ -220,6 +220,31 @@ int troute_sync(troute_handle* h, troute_stats* stats);
  * replays it on each troute_graph_launch (state carries over). */
 int troute_graph_capture(troute_handle* h, const double* qlat_ts_device, int n_ts);
 int troute_graph_launch(troute_handle* h, void* stream);
+/* ---- autotuner --------------------------------------------------------- */
+/* Times the handle's candidate launch configurations on a trial run of n_ts
+ * steps of qlat_ts_device (each trial from the same saved device state, the
+ * minimum of `repeats` runs) and keeps the fastest in the handle's cfg. The
+ * candidates: the ready-queue kernel (mapping 3) at every resident-block count
+ * from 1 to its occupancy, with and without item continuation; with
+ * TROUTE_TUNE_ALL_MAPPINGS also the per-lane refill kernel (mapping 2) at
+ * every block count and the one-block-per-warp kernel (mapping 1) at 32, 64
+ * and 128 threads per block (not with cfg.warm_start, which needs mapping 3).
+ * The schedule does not change results (bit-identical across shapes). The
+ * routing state is restored afterwards; a captured graph is released
+ * (capture again). */
+#define TROUTE_TUNE_ALL_MAPPINGS 1
+#define TROUTE_TUNE_MAX_TRIALS 32
+typedef struct troute_tune_result {
+    int mapping, blocks_per_sm, threads_per_block, schedule_flags;  /* chosen */
+    double best_ms;                  /* kernel time of the chosen configuration's trial */
+    double default_ms;               /* the default configuration's trial (mapping 3, full occupancy) */
+    int n_trials;
+    int trial_cfg[TROUTE_TUNE_MAX_TRIALS][4];  /* mapping, blocks per SM, threads, flags */
+    double trial_ms[TROUTE_TUNE_MAX_TRIALS];   /* -1: the trial failed */
+} troute_tune_result;
+int troute_autotune(troute_handle* h, const double* qlat_ts_device, int n_ts, int repeats, int flags,
+                    troute_tune_result* result);
+
 /* Per-step discharge history [n_ts][n_segments] of the last run (needs
  * cfg.record_history). */
 int troute_get_history(troute_handle* h, double* q_hist, int n_ts);
@@ -293,6 +318,31 @@ int troute_levels(int n_reaches, const int* reach_up_ptr, const int* reach_up_id
                   int* reach_level, int* level_ptr, int* level_reach, int* n_levels);
 /* Checks a topology; returns TROUTE_OK or TROUTE_ETOPO with a message. */
 int troute_validate(const troute_topo* topo);
+
+/* ---- linearised MC (approximate mode) --------------------------------- */
+/* The reference's linear form (water-prediction/t-route/wavefront/
+ * linear_mc.cu): fixed per-segment coefficients C1, C2, C3, C4/ql from the
+ * channel at half bankfull depth (linear_mc.cu:57-100), then per step
+ * Q_new = C1 Q_up_new + C2 Q_up_old + C3 Q_old + (C4/ql) qlat in topological
+ * order (cpu_linear_mc, :177-232), FP32. No secant iteration; the secant
+ * path is its judge. Every reach needs at least one segment. */
+typedef struct troute_linear troute_linear;
+/* Coefficients for n segments, computed on the device (FP32, CUDA powf/sqrtf
+ * as the reference's kernel_precompute_coeffs). Host arrays. */
+int troute_linear_coeffs(const troute_chparams_f32* params, int n_segments, double dt, float* c1, float* c2,
+                         float* c3, float* c4oq);
+int troute_linear_create(troute_linear** h, const troute_topo* topo, const float* c1, const float* c2,
+                         const float* c3, const float* c4oq);
+int troute_linear_destroy(troute_linear* h);
+/* n_ts steps of device lateral inflow [n_ts][n_segments] (float); q_dev
+ * [n_segments] holds the discharge before the run and after it. Synchronous;
+ * wait_cycles bounds each device wait without progress (0: ~4 s). */
+int troute_linear_run_device(troute_linear* h, const float* qlat_ts_device, int n_ts, float* q_device,
+                             long long wait_cycles, void* stream);
+/* One-shot host form of cpu_linear_mc's arguments: coefficients, lateral
+ * inflow [n_ts][n_segments], initial discharge -> final discharge. */
+int troute_linear_route(const troute_topo* topo, const float* c1, const float* c2, const float* c3,
+                        const float* c4oq, const float* qlat_ts, const float* q0, int n_ts, float* q_out);
 
 /* ---- on-disk network format ------------------------------------------- */
 /* The reference's topo.bin / params.bin / forcings.bin directory format

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -200,7 +201,7 @@ struct troute_handle {
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    int grid = 0, threads = 128, mapping = 2;
+    int grid = 0, threads = 128, mapping = 2, n_sms = 1;
     int last_n_ts = 0;
 
     cudaGraph_t graph = nullptr;
@@ -279,6 +280,7 @@ static int launch_shape(troute_handle* H)
         if ((rc = route_occupancy(H->threads, &bps))) return rc;
     }
     if (H->cfg.blocks_per_sm > 0) bps = std::min(bps, H->cfg.blocks_per_sm);
+    H->n_sms = std::max(1, sms);
     H->grid = std::max(1, sms * std::max(1, bps));
     return TROUTE_OK;
 }
@@ -1149,6 +1151,135 @@ struct CkptHeader {
     int version, R, S, pad;
     long long steps;
 };
+
+// ---- autotuner -----------------------------------------------------------
+// The routing state a run changes, copied device-to-device so every trial of
+// the tuner starts from the same state and the handle's state is untouched by
+// tuning.
+struct DevSnapshot {
+    DBuf<double> q, d, v, ring;
+    DBuf<int> done, step_base;
+    long long steps = 0;
+};
+
+static int snapshot_copy(troute_handle* H, DevSnapshot& S, bool save)
+{
+    int rc;
+    if (save && ((rc = S.q.alloc(H->q.n)) || (rc = S.d.alloc(H->d.n)) || (rc = S.v.alloc(H->v.n)) ||
+                 (rc = S.ring.alloc(H->ring.n)) || (rc = S.done.alloc(H->done.n)) ||
+                 (rc = S.step_base.alloc(H->step_base.n))))
+        return rc;
+    const cudaStream_t st = H->stream;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        return bytes ? cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st), "snapshot") : 0;
+    };
+    if (save) {
+        if ((rc = cp(S.q.p, H->q.p, H->q.n * 8)) || (rc = cp(S.d.p, H->d.p, H->d.n * 8)) ||
+            (rc = cp(S.v.p, H->v.p, H->v.n * 8)) || (rc = cp(S.ring.p, H->ring.p, H->ring.n * 8)) ||
+            (rc = cp(S.done.p, H->done.p, H->done.n * 4)) || (rc = cp(S.step_base.p, H->step_base.p, H->step_base.n * 4)))
+            return rc;
+        S.steps = H->steps_done;
+    } else {
+        if ((rc = cp(H->q.p, S.q.p, H->q.n * 8)) || (rc = cp(H->d.p, S.d.p, H->d.n * 8)) ||
+            (rc = cp(H->v.p, S.v.p, H->v.n * 8)) || (rc = cp(H->ring.p, S.ring.p, H->ring.n * 8)) ||
+            (rc = cp(H->done.p, S.done.p, H->done.n * 4)) || (rc = cp(H->step_base.p, S.step_base.p, H->step_base.n * 4)))
+            return rc;
+        H->steps_done = S.steps;
+        H->broken = false;
+    }
+    return cuda_check(cudaStreamSynchronize(st), "snapshot sync");
+}
+
+static int occupancy_of(int mapping, int threads, bool warm, int* bps)
+{
+    if (mapping == 3) return route_dataflow_occupancy(bps, warm);
+    if (mapping == 2) return route_pool_occupancy(bps);
+    return route_occupancy(threads, bps);
+}
+
+extern "C" int troute_autotune(troute_handle* h, const double* qlat_ts_device, int n_ts, int repeats, int flags,
+                               troute_tune_result* res)
+{
+    if (!h || !qlat_ts_device || !res) return set_error(TROUTE_EINVAL, "null argument");
+    if (n_ts < 1 || repeats < 1) return set_error(TROUTE_EINVAL, "n_ts and repeats must be positive");
+    if (h->broken) return set_error(TROUTE_ESTATE, "handle unusable after an earlier device failure");
+    std::memset(res, 0, sizeof *res);
+    const troute_cfg base = h->cfg;
+    const bool warm = base.warm_start != 0;
+    // candidate launch configurations: {mapping, blocks_per_sm, threads_per_block, schedule_flags}
+    std::vector<std::array<int, 4>> cand;
+    int rc, occ = 0;
+    if ((rc = occupancy_of(3, 128, warm, &occ))) return rc;
+    const int occ3 = std::max(1, occ);
+    for (int b = 1; b <= std::max(1, occ); ++b)
+        for (int f = 0; f < 2; ++f) cand.push_back({3, b, 128, f});
+    if (!warm && (flags & TROUTE_TUNE_ALL_MAPPINGS)) {
+        if ((rc = occupancy_of(2, 128, false, &occ))) return rc;
+        for (int b = 1; b <= std::max(1, occ); ++b) cand.push_back({2, b, 128, 0});
+        for (int t : {32, 64, 128}) cand.push_back({1, 0, t, 0});
+    }
+    if ((int)cand.size() > TROUTE_TUNE_MAX_TRIALS) cand.resize(TROUTE_TUNE_MAX_TRIALS);
+    // the tuner's own graph-free runs; a captured graph no longer matches the shape
+    if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+    }
+    if (h->graph) {
+        cudaGraphDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    DevSnapshot snap;
+    if ((rc = snapshot_copy(h, snap, true))) return rc;
+    int best = -1;
+    double best_ms = 0.0;
+    for (size_t i = 0; i < cand.size(); ++i) {
+        troute_cfg c = base;
+        c.mapping = cand[i][0];
+        c.blocks_per_sm = cand[i][1];
+        c.threads_per_block = cand[i][0] == 1 ? cand[i][2] : 0;
+        c.schedule_flags = (base.schedule_flags & ~1) | cand[i][3];
+        c.record_history = c.record_pairs = c.record_start = 0;
+        h->cfg = c;
+        double ms = -1.0;
+        if ((rc = launch_shape(h)) == TROUTE_OK) {
+            for (int r = 0; r < repeats; ++r) {
+                if ((rc = snapshot_copy(h, snap, false))) break;
+                troute_stats st;
+                if ((rc = troute_run_device(h, qlat_ts_device, n_ts, nullptr))) break;
+                if ((rc = troute_sync(h, &st))) break;
+                if (ms < 0.0 || st.kernel_ms < ms) ms = st.kernel_ms;
+            }
+        }
+        res->trial_cfg[i][0] = cand[i][0];
+        res->trial_cfg[i][1] = h->grid / std::max(1, h->n_sms);
+        res->trial_cfg[i][2] = h->threads;
+        res->trial_cfg[i][3] = cand[i][3];
+        res->trial_ms[i] = rc == TROUTE_OK ? ms : -1.0;
+        res->n_trials = (int)i + 1;
+        if (rc != TROUTE_OK) continue;  // a failing shape (e.g. a wait that ran out) is skipped
+        if (best < 0 || ms < best_ms) {
+            best = (int)i;
+            best_ms = ms;
+        }
+        if (cand[i][0] == 3 && cand[i][1] == occ3 && cand[i][3] == 0) res->default_ms = ms;
+    }
+    h->cfg = base;
+    if (best >= 0) {
+        h->cfg.mapping = cand[best][0];
+        h->cfg.blocks_per_sm = cand[best][1];
+        h->cfg.threads_per_block = cand[best][0] == 1 ? cand[best][2] : 0;
+        h->cfg.schedule_flags = (base.schedule_flags & ~1) | cand[best][3];
+    }
+    if ((rc = launch_shape(h))) return rc;
+    if ((rc = snapshot_copy(h, snap, false))) return rc;
+    if (best < 0) return set_error(TROUTE_ECUDA, "no launch configuration completed a trial run");
+    res->mapping = h->cfg.mapping;
+    res->blocks_per_sm = h->grid / std::max(1, h->n_sms);
+    res->threads_per_block = h->threads;
+    res->schedule_flags = h->cfg.schedule_flags;
+    res->best_ms = best_ms;
+    return TROUTE_OK;
+}
 
 extern "C" int troute_checkpoint(troute_handle* h, void* buf, size_t* nbytes)
 {

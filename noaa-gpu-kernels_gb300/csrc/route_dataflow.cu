@@ -36,6 +36,10 @@ constexpr unsigned kFullMask = 0xffffffffu;
 constexpr int L_FETCH = L_WAIT;  // claimed a queue slot, waiting for it to be written
 constexpr unsigned long long kWakeItems = 16;  // queued items that wake an idle warp
 constexpr long long kWakeCycles = 8000;        // ... or this long unclaimed (~4 us)
+#ifndef TROUTE_SLEEP_MAX_NS
+#define TROUTE_SLEEP_MAX_NS 3200
+#endif
+constexpr unsigned kSleepMinNs = 200, kSleepMaxNs = TROUTE_SLEEP_MAX_NS;  // idle-warp polling back-off
 
 __device__ __forceinline__ unsigned lanemask_lt_df()
 {
@@ -168,6 +172,7 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
     Lane L;
     L.mode = L_IDLE;
     unsigned long long n_pass = 0, n_busy = 0, n_wait = 0, n_idle = 0;
+    unsigned idle_ns = kSleepMinNs;  // warp-uniform
 
     while (true) {
         // ---- idle lanes claim queue slots (one atomic per warp) ----
@@ -339,7 +344,20 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
             }
         }
         if (__any_sync(kFullMask, failed)) break;
-        if (__ballot_sync(kFullMask, L.mode >= L_SOLVE) == 0) __nanosleep(200);
+        // a warp without solving lanes sleeps before polling again: briefly when
+        // it holds claimed slots (their items are about to be written), with a
+        // doubling back-off while it finds nothing at all, so that idle warps
+        // do not crowd the queue counters' L2 lines while others solve
+        if (__ballot_sync(kFullMask, L.mode >= L_SOLVE) == 0) {
+            if (__any_sync(kFullMask, L.mode == L_FETCH)) {
+                __nanosleep(kSleepMinNs);
+            } else {
+                __nanosleep(idle_ns);
+                idle_ns = idle_ns < kSleepMaxNs ? 2 * idle_ns : kSleepMaxNs;
+            }
+        } else {
+            idle_ns = kSleepMinNs;
+        }
     }
     if (lane == 0) {
         atomicAdd(&run.stats->warp_passes, n_pass);

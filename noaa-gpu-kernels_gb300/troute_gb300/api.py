@@ -155,6 +155,12 @@ _SIGS = {
     "troute_set_warm_start": ([_P, _P, _D], _I),
     "troute_get_pairs": ([_P, _P, C.c_longlong, _P], _I),
     "troute_get_start_history": ([_P, _P, _I], _I),
+    "troute_autotune": ([_P, _P, _I, _I, _I, _P], _I),
+    "troute_linear_coeffs": ([_P, _I, _D, _P, _P, _P, _P], _I),
+    "troute_linear_create": ([_P, _P, _P, _P, _P, _P], _I),
+    "troute_linear_destroy": ([_P], _I),
+    "troute_linear_run_device": ([_P, _P, _I, _P, C.c_longlong, _P], _I),
+    "troute_linear_route": ([_P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
     "troute_read_network": ([C.c_char_p, _P], _I),
     "troute_free_network": ([_P], None),
     "troute_write_network": ([C.c_char_p, _P], _I),
@@ -454,6 +460,14 @@ class Network:
         _check(lib().troute_get_history(self._h, _ptr(out), int(n_ts)))
         return out
 
+    def autotune(self, qlat_dev_ptr: int, n_ts: int, repeats: int = 1, all_mappings: bool = True) -> dict:
+        """Times the candidate launch configurations on n_ts steps of the device
+        lateral inflow at qlat_dev_ptr and keeps the fastest (state unchanged)."""
+        r = TuneResult()
+        _check(lib().troute_autotune(self._h, C.c_void_p(qlat_dev_ptr), int(n_ts), int(repeats),
+                                     TUNE_ALL_MAPPINGS if all_mappings else 0, C.byref(r)))
+        return r.as_dict()
+
     def set_warm_start(self, model: "WarmModel | None", delta: float = 0.05):
         """Attaches a trained model (None detaches); runs use it with cfg.warm_start = 1."""
         self._warm = model
@@ -482,6 +496,24 @@ class Network:
     def restore(self, blob: bytes):
         buf = C.create_string_buffer(blob, len(blob))
         _check(lib().troute_restore(self._h, buf, len(blob)))
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("mapping", C.c_int), ("blocks_per_sm", C.c_int), ("threads_per_block", C.c_int),
+                ("schedule_flags", C.c_int), ("best_ms", C.c_double), ("default_ms", C.c_double),
+                ("n_trials", C.c_int), ("trial_cfg", (C.c_int * 4) * 32), ("trial_ms", C.c_double * 32)]
+
+    def as_dict(self) -> dict:
+        n = self.n_trials
+        return {"mapping": self.mapping, "blocks_per_sm": self.blocks_per_sm,
+                "threads_per_block": self.threads_per_block, "schedule_flags": self.schedule_flags,
+                "best_ms": self.best_ms, "default_ms": self.default_ms,
+                "trials": [{"mapping": self.trial_cfg[i][0], "blocks_per_sm": self.trial_cfg[i][1],
+                            "threads": self.trial_cfg[i][2], "flags": self.trial_cfg[i][3], "ms": self.trial_ms[i]}
+                           for i in range(n)]}
+
+
+TUNE_ALL_MAPPINGS = 1
 
 
 class NetFile(C.Structure):
@@ -544,6 +576,70 @@ def write_network(path: str, net: dict):
         setattr(n, k, arr(k, np.float32))
     os.makedirs(path, exist_ok=True)
     _check(lib().troute_write_network(os.fsencode(path), C.byref(n)))
+
+
+def _f32_params(p):
+    p = np.ascontiguousarray(p)
+    if p.dtype != CHPARAMS_F32_DTYPE:
+        p = np.ascontiguousarray(np.asarray(p, np.float32).reshape(-1, 8)).view(CHPARAMS_F32_DTYPE).reshape(-1)
+    return p
+
+
+def linear_coeffs(params_f32, dt: float = 300.0):
+    """Linearised-MC coefficients (C1, C2, C3, C4/ql), float32, computed on the device."""
+    p = _f32_params(params_f32)
+    n = p.shape[0]
+    c = [np.zeros(n, np.float32) for _ in range(4)]
+    _check(lib().troute_linear_coeffs(_ptr(p), n, float(dt), *(_ptr(x) for x in c)))
+    return c
+
+
+def linear_route(topo: dict, coeffs, qlat_ts, q0):
+    """cpu_linear_mc drop-in on the GPU: float coefficients, lateral inflow
+    [n_ts][n_segments] and initial discharge -> final discharge (float32)."""
+    S = int(topo["n_segments"])
+    t = _topo_struct(topo["reach_seg_start"], topo["reach_seg_len"], topo["reach_up_ptr"], topo["reach_up_idx"], S)
+    cs = [np.ascontiguousarray(c, np.float32) for c in coeffs]
+    ql = np.ascontiguousarray(qlat_ts, np.float32)
+    q = np.ascontiguousarray(q0, np.float32)
+    out = np.zeros(S, np.float32)
+    _check(lib().troute_linear_route(C.byref(t[0]), *(_ptr(c) for c in cs), _ptr(ql), _ptr(q), int(ql.shape[0]),
+                                     _ptr(out)))
+    return out
+
+
+class LinearNetwork:
+    """Persistent device form of the linearised MC (troute_linear_*)."""
+
+    def __init__(self, topo: dict, coeffs):
+        S = int(topo["n_segments"])
+        self._t = _topo_struct(topo["reach_seg_start"], topo["reach_seg_len"], topo["reach_up_ptr"],
+                               topo["reach_up_idx"], S)
+        cs = [np.ascontiguousarray(c, np.float32) for c in coeffs]
+        self._h = C.c_void_p()
+        _check(lib().troute_linear_create(C.byref(self._h), C.byref(self._t[0]), *(_ptr(c) for c in cs)))
+        self.n_segments = S
+
+    def run_device(self, qlat_dev_ptr: int, n_ts: int, q_dev_ptr: int, wait_cycles: int = 0, stream: int = 0):
+        _check(lib().troute_linear_run_device(self._h, C.c_void_p(qlat_dev_ptr), int(n_ts), C.c_void_p(q_dev_ptr),
+                                              int(wait_cycles), C.c_void_p(stream)))
+
+    def close(self):
+        if self._h:
+            lib().troute_linear_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 WARM_NPARAMS = 4801

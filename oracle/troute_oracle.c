@@ -577,3 +577,96 @@ int oracle_route_tree_it(const int* reach_seg_start, const int* reach_seg_len,
     if (iters_total) *iters_total = o.iters_total;
     return rc;
 }
+
+/* ---------------------------------------------------------------------------
+ * Linearised MC (water-prediction/t-route/wavefront/linear_mc.cu).
+ * oracle_linear_coeffs follows compute_mc_coeffs (:57-100) in float with the
+ * C library's powf/sqrtf (the reference evaluates it on the GPU with CUDA's;
+ * the two differ in the last bits, so the GPU coefficients are compared with a
+ * tolerance). oracle_linear_route follows cpu_linear_mc (:177-232): given the
+ * same coefficients it is the reference's float arithmetic, operation for
+ * operation (no contraction).
+ * ------------------------------------------------------------------------- */
+void oracle_linear_coeffs(const oracle_chparams_f32* params, int n, float dt, float* c1, float* c2, float* c3,
+                          float* c4oq)
+{
+    for (int i = 0; i < n; ++i) {
+        const oracle_chparams_f32 p = params[i];
+        const float z = (p.cs == 0.0f) ? 1.0f : 1.0f / p.cs;
+        float bfd;
+        if (p.bw > p.tw) bfd = p.bw / 0.00001f;
+        else if (p.bw == p.tw) bfd = p.bw / (2.0f * z);
+        else bfd = (p.tw - p.bw) / (2.0f * z);
+        const float h = fmaxf(0.5f * bfd, 0.1f);
+        const float twl = p.bw + 2.0f * z * h;
+        const float A = (p.bw + h * z) * h;
+        const float WP = p.bw + 2.0f * h * sqrtf(1.0f + z * z);
+        const float R = (WP > 0.0f) ? A / WP : 0.0f;
+        const float r23 = powf(R, 2.0f / 3.0f);
+        const float r53 = powf(R, 5.0f / 3.0f);
+        const float Ck = fmaxf(1e-6f, (sqrtf(p.s0) / p.n_ch) *
+                                          ((5.0f / 3.0f) * r23 -
+                                           (2.0f / 3.0f) * r53 * (2.0f * sqrtf(1.0f + z * z) / (p.bw + 2.0f * h * z))));
+        const float Km = fmaxf(dt, p.dx / Ck);
+        const float tw_use = (h > bfd && p.twcc > 0.0f) ? p.twcc : twl;
+        float X = 0.25f;
+        if (Ck > 0.0f && tw_use * p.s0 * Ck * p.dx > 0.0f)
+            X = fminf(0.5f, fmaxf(0.0f, 0.5f * (1.0f - 0.0f / (2.0f * tw_use * p.s0 * Ck * p.dx))));
+        float D = Km * (1.0f - X) + dt / 2.0f;
+        if (D == 0.0f) D = 1.0f;
+        c1[i] = (Km * X + dt / 2.0f) / D;
+        c2[i] = (dt / 2.0f - Km * X) / D;
+        c3[i] = (Km * (1.0f - X) - dt / 2.0f) / D;
+        c4oq[i] = dt / D;
+    }
+}
+
+int oracle_linear_route(const float* c1, const float* c2, const float* c3, const float* c4oq,
+                        const int* reach_seg_start, const int* reach_seg_len, const int* reach_up_ptr,
+                        const int* reach_up_idx, const int* level_ptr, const int* level_reach, int n_reaches,
+                        int n_levels, int n_segments, const float* qlat_ts, const float* q0, float* q_final,
+                        int n_ts)
+{
+    (void)n_reaches;
+    float* Qp = (float*)malloc((size_t)(n_segments ? n_segments : 1) * sizeof(float));
+    float* Qn = (float*)calloc((size_t)(n_segments ? n_segments : 1), sizeof(float));
+    if (!Qp || !Qn) {
+        free(Qp);
+        free(Qn);
+        return 2;
+    }
+    memcpy(Qp, q0, (size_t)n_segments * sizeof(float));
+    for (int t = 0; t < n_ts; ++t) {
+        const float* qlat = qlat_ts + (size_t)t * (size_t)n_segments;
+        for (int L = 0; L < n_levels; ++L) {
+            for (int kk = level_ptr[L]; kk < level_ptr[L + 1]; ++kk) {
+                const int r = level_reach[kk];
+                const int s0 = reach_seg_start[r], sl = reach_seg_len[r];
+                float sum_new = 0.f, sum_old = 0.f;
+                for (int k = reach_up_ptr[r]; k < reach_up_ptr[r + 1]; ++k) {
+                    const int u = reach_up_idx[k];
+                    const int last_u = reach_seg_start[u] + reach_seg_len[u] - 1;
+                    sum_new += Qn[last_u];
+                    sum_old += Qp[last_u];
+                }
+                /* the first segment takes the upstream sums, the others the
+                 * previous segment's new and old discharge */
+                float pn = sum_new, po = sum_old;
+                for (int i = 0; i < sl; ++i) {
+                    const int idx = s0 + i;
+                    Qn[idx] = c1[idx] * pn + c2[idx] * po + c3[idx] * Qp[idx] + c4oq[idx] * qlat[idx];
+                    pn = Qn[idx];
+                    po = Qp[idx];
+                }
+            }
+        }
+        float* tmp = Qp;
+        Qp = Qn;
+        Qn = tmp;
+        memset(Qn, 0, (size_t)n_segments * sizeof(float));
+    }
+    memcpy(q_final, Qp, (size_t)n_segments * sizeof(float));
+    free(Qp);
+    free(Qn);
+    return 0;
+}

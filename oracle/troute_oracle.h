@@ -125,6 +125,22 @@ int oracle_route_tree_ex(const int* reach_seg_start, const int* reach_seg_len,
                          double* q_out, double* d_out, double* v_out,
                          double* reach_last_out, oracle_tree_opts* opts);
 
+/* Float parameter record of params.bin (wavefront_mc.cu:41-44). */
+typedef struct oracle_chparams_f32 {
+    float dx, bw, tw, twcc, n_ch, ncc, cs, s0;
+} oracle_chparams_f32;
+
+/* Linearised MC (linear_mc.cu): coefficients (compute_mc_coeffs, :57-100) and
+ * the float routing of cpu_linear_mc (:177-232); every reach needs at least
+ * one segment. */
+void oracle_linear_coeffs(const oracle_chparams_f32* params, int n, float dt, float* c1, float* c2, float* c3,
+                          float* c4oq);
+int oracle_linear_route(const float* c1, const float* c2, const float* c3, const float* c4oq,
+                        const int* reach_seg_start, const int* reach_seg_len, const int* reach_up_ptr,
+                        const int* reach_up_idx, const int* level_ptr, const int* level_reach, int n_reaches,
+                        int n_levels, int n_segments, const float* qlat_ts, const float* q0, float* q_final,
+                        int n_ts);
+
 #ifdef __cplusplus
 }
 #endif

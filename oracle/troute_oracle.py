@@ -69,6 +69,10 @@ def oracle():
         L.oracle_mc_solve_warm.argtypes = ([C.c_double] * 5 + [_P, C.c_double, _P, C.c_double, C.c_double, C.c_int]
                                            + [_P] * 4)
         L.oracle_mc_solve_warm.restype = C.c_double
+        L.oracle_linear_coeffs.argtypes = [_P, C.c_int, C.c_float] + [_P] * 4
+        L.oracle_linear_coeffs.restype = None
+        L.oracle_linear_route.argtypes = [_P] * 10 + [C.c_int] * 3 + [_P] * 3 + [C.c_int]
+        L.oracle_linear_route.restype = C.c_int
         L.oracle_set_pow_mode.argtypes = [C.c_int]
         L.oracle_set_pow_mode.restype = None
         L.oracle_pow23_53.argtypes = [C.c_double, _P, _P]
@@ -111,6 +115,10 @@ def ref():
         L.ref_cpu_mc.restype = None
         L.ref_cpu_wavefront_fp64.argtypes = [_P] * 7 + [C.c_int] * 3 + [_P] * 6 + [C.c_int, C.c_double]
         L.ref_cpu_wavefront_fp64.restype = None
+        L.ref_linear_coeffs.argtypes = [_P, C.c_int, C.c_float] + [_P] * 4
+        L.ref_linear_coeffs.restype = None
+        L.ref_cpu_linear_mc.argtypes = [_P] * 10 + [C.c_int] * 3 + [_P] * 3 + [C.c_int]
+        L.ref_cpu_linear_mc.restype = None
         _REF = L
     return _REF
 
@@ -279,3 +287,53 @@ def ref_wavefront_fp64(topo, params_f32, qlat_f32, qdp0_f32, dp0_f32, reach_last
                                  _ptr(level_ptr), _ptr(level_reach), R, level_ptr.size - 1, S, _ptr(ql), _ptr(q0),
                                  _ptr(d0), _ptr(r0), _ptr(q), _ptr(rl), int(ql.shape[0]), float(dt))
     return q, rl
+
+
+def _params_f32(p):
+    p = np.ascontiguousarray(p)
+    if p.dtype != CHP32:
+        p = np.ascontiguousarray(np.asarray(p, np.float32).reshape(-1, 8)).view(CHP32).reshape(-1)
+    return p
+
+
+def linear_coeffs(params_f32, dt=300.0, use_ref=False):
+    """Linearised-MC coefficients (C1, C2, C3, C4/ql) per segment: the oracle's
+    restatement of compute_mc_coeffs, or (use_ref) the reference's own."""
+    p = _params_f32(params_f32)
+    n = p.shape[0]
+    c = [np.zeros(n, np.float32) for _ in range(4)]
+    f = ref().ref_linear_coeffs if use_ref else oracle().oracle_linear_coeffs
+    f(_ptr(p), n, float(dt), *(_ptr(x) for x in c))
+    return c
+
+
+def _linear_args(coeffs, topo, level_ptr, level_reach):
+    seg_start = np.ascontiguousarray(topo["reach_seg_start"], np.int32)
+    seg_len = np.ascontiguousarray(topo["reach_seg_len"], np.int32)
+    up_ptr = np.ascontiguousarray(topo["reach_up_ptr"], np.int32)
+    up_idx = np.ascontiguousarray(topo["reach_up_idx"] if len(topo["reach_up_idx"]) else [0], np.int32)
+    R = seg_start.size
+    if level_ptr is None:
+        level_ptr, level_reach = levels(up_ptr, up_idx, R)
+    lp = np.ascontiguousarray(level_ptr, np.int32)
+    lr = np.ascontiguousarray(level_reach, np.int32)
+    cs = [np.ascontiguousarray(c, np.float32) for c in coeffs]
+    return cs, [seg_start, seg_len, up_ptr, up_idx, lp, lr], R, lp.size - 1
+
+
+def linear_route(coeffs, topo, qlat_ts, q0, level_ptr=None, level_reach=None, use_ref=False):
+    """Float routing of cpu_linear_mc: the oracle's restatement or (use_ref)
+    the reference's own; returns the final discharge."""
+    cs, ints, R, L = _linear_args(coeffs, topo, level_ptr, level_reach)
+    S = int(topo["n_segments"])
+    ql = np.ascontiguousarray(qlat_ts, np.float32)
+    q0 = np.ascontiguousarray(q0, np.float32)
+    out = np.zeros(S, np.float32)
+    args = [_ptr(x) for x in cs] + [_ptr(x) for x in ints] + [R, L, S, _ptr(ql), _ptr(q0), _ptr(out), ql.shape[0]]
+    if use_ref:
+        ref().ref_cpu_linear_mc(*args)
+    else:
+        rc = oracle().oracle_linear_route(*args)
+        if rc:
+            raise RuntimeError(f"oracle_linear_route failed: {rc}")
+    return out

@@ -5,7 +5,10 @@ generate_params, generate_forcings, write_network, write_params,
 write_forcings), and tests/golden/refnet_out.npz with the reference's own
 cpu_wavefront_fp64 (water-prediction/t-route/wavefront/wavefront_mc.cu:495-564,
 compiled unmodified into oracle/_ref/libtroute_ref.so by make -C oracle ref)
-routing those files: final discharge and reach outflow after 1 and 12 steps.
+routing those files: final discharge and reach outflow after 1 and 12 steps;
+and the reference's linearised form (linear_mc.cu): its coefficients
+(compute_mc_coeffs, host instance) and cpu_linear_mc's final discharge after
+the 12 steps.
 
 The network is small (target 300 reaches, 12 steps, seed 7) so the files stay
 a few hundred KB. This script needs the reference checkout and only runs in
@@ -52,6 +55,13 @@ def main(ref_root: str):
         q, rl = O.ref_wavefront_fp64(topo, n["params"], n["qlat"][:steps], n["qdp0"], n["dp0"], n["qup0"],
                                      level_ptr=n["level_ptr"], level_reach=n["level_reach"])
         out[f"q_{steps}"], out[f"reach_last_{steps}"] = q, rl
+    # the linearised form (linear_mc.cu): the reference's coefficient function
+    # (host instance) and its cpu_linear_mc over all steps from qdp0
+    c = O.linear_coeffs(n["params"], 300.0, use_ref=True)
+    for k, v in zip(("lin_c1", "lin_c2", "lin_c3", "lin_c4oq"), c):
+        out[k] = v
+    out["lin_q"] = O.linear_route(c, topo, n["qlat"], n["qdp0"], level_ptr=n["level_ptr"],
+                                  level_reach=n["level_reach"], use_ref=True)
     np.savez_compressed(os.path.join(HERE, "refnet_out.npz"), **out)
     print(f"refnet: {n['n_reaches']} reaches, {n['n_segments']} segments, {n['n_levels']} levels, "
           f"{n['n_ts']} steps")

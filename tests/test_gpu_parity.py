@@ -332,3 +332,35 @@ def test_graph_replay_equals_runs():
         qr = r.get_state()
     for x, y in zip(qg, qr):
         np.testing.assert_array_equal(x, y)
+
+
+def test_autotuner_keeps_state_and_results():
+    """The tuner times every candidate shape from the same saved state, keeps
+    the fastest, leaves the routing state as it was, and the tuned handle
+    routes bit-identically to an untuned one."""
+    torch = pytest.importorskip("torch")
+    c = synth.network("tree:20000", seed=21, n_ts=8)
+    ql = torch.from_numpy(np.ascontiguousarray(c["qlat"])).cuda()
+    cfg = cfg_of(TIGHT)
+    with T.Network(c["topo"], c["params"], cfg=cfg) as a:
+        a.set_state(c["q0"], c["d0"], c["rl0"])
+        a.run(c["qlat"][:3])
+        before = a.get_state()
+        res = a.autotune(ql.data_ptr(), 8, repeats=1, all_mappings=True)
+        after = a.get_state()
+        for x, y in zip(before, after):
+            np.testing.assert_array_equal(x, y)
+        assert a.steps_done == 3
+        assert len(res["trials"]) >= 6
+        assert all(t["ms"] > 0 for t in res["trials"])
+        assert {t["mapping"] for t in res["trials"]} == {1, 2, 3}
+        assert res["best_ms"] == min(t["ms"] for t in res["trials"])
+        a.run(c["qlat"])
+        qa = a.get_state()
+    with T.Network(c["topo"], c["params"], cfg=cfg) as b:
+        b.set_state(c["q0"], c["d0"], c["rl0"])
+        b.run(c["qlat"][:3])
+        b.run(c["qlat"])
+        qb = b.get_state()
+    for x, y in zip(qa, qb):
+        np.testing.assert_array_equal(x, y)
