@@ -344,6 +344,29 @@ int troute_linear_run_device(troute_linear* h, const float* qlat_ts_device, int 
 int troute_linear_route(const troute_topo* topo, const float* c1, const float* c2, const float* c3,
                         const float* c4oq, const float* qlat_ts, const float* q0, int n_ts, float* q_out);
 
+/* ---- diffusive-wave tridiagonal step ----------------------------------- */
+/* The reference's t-route diffusive-wave solver (water-prediction/
+ * owp_extended_kernels.cu:24-153, cpu_diffusive_tridiag / kernel_diffusive_
+ * tridiag): per reach a Crank-Nicolson tridiagonal system over its ncomp
+ * computational nodes, forward elimination and back substitution, FP32.
+ * Arrays are [n_reaches][max_nodes] (the reference's MAX_NODES is 500); nodes
+ * at or past a reach's ncomp are neither read nor written. Bit-identical to
+ * the reference's CPU routine. celerity is accepted for the argument list
+ * and not read (the reference computes an unused Courant number from it). */
+typedef struct troute_diff_reach {
+    int ncomp;     /* computational nodes, 1..max_nodes */
+    float theta;   /* Crank-Nicolson weight */
+    float dtini;   /* time step, s */
+} troute_diff_reach;
+int troute_diffusive_tridiag(const troute_diff_reach* reaches, const float* dx, const float* diffusivity,
+                             const float* celerity, const float* qp_prev, float* qp_out, int n_reaches,
+                             int max_nodes);
+/* Device arrays; scratch holds 2 * n_reaches * max_nodes floats; asynchronous
+ * on `stream`. */
+int troute_diffusive_tridiag_device(const troute_diff_reach* reaches, const float* dx, const float* diffusivity,
+                                    const float* celerity, const float* qp_prev, float* qp_out, int n_reaches,
+                                    int max_nodes, float* scratch, void* stream);
+
 /* ---- on-disk network format ------------------------------------------- */
 /* The reference's topo.bin / params.bin / forcings.bin directory format
  * (water-prediction/t-route/wavefront/gen_network.py:292-337, read by

@@ -156,6 +156,8 @@ _SIGS = {
     "troute_get_pairs": ([_P, _P, C.c_longlong, _P], _I),
     "troute_get_start_history": ([_P, _P, _I], _I),
     "troute_autotune": ([_P, _P, _I, _I, _I, _P], _I),
+    "troute_diffusive_tridiag": ([_P] * 6 + [_I, _I], _I),
+    "troute_diffusive_tridiag_device": ([_P] * 6 + [_I, _I, _P, _P], _I),
     "troute_linear_coeffs": ([_P, _I, _D, _P, _P, _P, _P], _I),
     "troute_linear_create": ([_P, _P, _P, _P, _P, _P], _I),
     "troute_linear_destroy": ([_P], _I),
@@ -605,6 +607,21 @@ def linear_route(topo: dict, coeffs, qlat_ts, q0):
     out = np.zeros(S, np.float32)
     _check(lib().troute_linear_route(C.byref(t[0]), *(_ptr(c) for c in cs), _ptr(ql), _ptr(q), int(ql.shape[0]),
                                      _ptr(out)))
+    return out
+
+
+DIFF_REACH_DTYPE = np.dtype([("ncomp", "<i4"), ("theta", "<f4"), ("dtini", "<f4")])
+
+
+def diffusive_tridiag(reaches, dx, diffusivity, qp_prev, qp_out=None, celerity=None):
+    """cpu_diffusive_tridiag drop-in on the GPU: [n_reaches][max_nodes] float
+    arrays, reaches with (ncomp, theta, dtini); returns qp_out."""
+    rp = np.ascontiguousarray(reaches, DIFF_REACH_DTYPE)
+    dx, df, qp = (np.ascontiguousarray(a, np.float32) for a in (dx, diffusivity, qp_prev))
+    n, m = qp.shape
+    out = np.zeros_like(qp) if qp_out is None else np.ascontiguousarray(qp_out, np.float32).copy()
+    cel = None if celerity is None else np.ascontiguousarray(celerity, np.float32)
+    _check(lib().troute_diffusive_tridiag(_ptr(rp), _ptr(dx), _ptr(df), _ptr(cel), _ptr(qp), _ptr(out), n, m))
     return out
 
 

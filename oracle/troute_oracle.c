@@ -670,3 +670,56 @@ int oracle_linear_route(const float* c1, const float* c2, const float* c3, const
     free(Qn);
     return 0;
 }
+
+/* ---------------------------------------------------------------------------
+ * Diffusive-wave tridiagonal step (water-prediction/owp_extended_kernels.cu:
+ * 24-91, cpu_diffusive_tridiag): float, the reference's operation order.
+ * Arrays [n_reaches][max_nodes]; nodes at or past ncomp untouched.
+ * ------------------------------------------------------------------------- */
+int oracle_diffusive_tridiag(const oracle_diff_reach* rp, const float* dx, const float* diffusivity,
+                             const float* qp_prev, float* qp_out, int n_reaches, int max_nodes)
+{
+    float* eei = (float*)malloc((size_t)(max_nodes > 0 ? max_nodes : 1) * sizeof(float));
+    float* ffi = (float*)malloc((size_t)(max_nodes > 0 ? max_nodes : 1) * sizeof(float));
+    if (!eei || !ffi) {
+        free(eei);
+        free(ffi);
+        return 2;
+    }
+    for (int j = 0; j < n_reaches; j++) {
+        const int nc = rp[j].ncomp;
+        const float theta = rp[j].theta, dtini = rp[j].dtini;
+        const size_t base = (size_t)j * (size_t)max_nodes;
+        if (nc < 1 || nc > max_nodes) {
+            free(eei);
+            free(ffi);
+            return 1;
+        }
+        eei[0] = 1.0f;
+        ffi[0] = 0.0f;
+        for (int i = 1; i < nc; i++) {
+            float dxi = dx[base + i - 1];
+            if (dxi < 1.0f) dxi = 1.0f;
+            const float alpha = 1.0f;
+            float diff_i = diffusivity[base + i];
+            if (diff_i < 0.01f) diff_i = 0.01f;
+            const float ppi = -theta * diff_i * dtini / (dxi * dxi) * 2.0f / (alpha * (alpha + 1.0f)) * alpha;
+            const float qqi = 1.0f - ppi * (alpha + 1.0f) / alpha;
+            const float rri = ppi / alpha;
+            const float qnext = (i < nc - 1) ? qp_prev[base + i + 1] : qp_prev[base + i];
+            const float ssi = qp_prev[base + i] + dtini * diff_i * (1.0f - theta) *
+                                                      (qp_prev[base + i - 1] - 2.0f * qp_prev[base + i] + qnext) /
+                                                      (dxi * dxi);
+            float denom = ppi * eei[i - 1] + qqi;
+            if (fabsf(denom) < 1e-20f) denom = 1e-20f;
+            eei[i] = -rri / denom;
+            ffi[i] = (ssi - ppi * ffi[i - 1]) / denom;
+        }
+        /* downstream boundary: the ghost node takes the previous discharge */
+        qp_out[base + nc - 1] = eei[nc - 1] * qp_prev[base + nc - 1] + ffi[nc - 1];
+        for (int i = nc - 2; i >= 0; i--) qp_out[base + i] = eei[i] * qp_out[base + i + 1] + ffi[i];
+    }
+    free(eei);
+    free(ffi);
+    return 0;
+}

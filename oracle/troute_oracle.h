@@ -141,6 +141,16 @@ int oracle_linear_route(const float* c1, const float* c2, const float* c3, const
                         int n_levels, int n_segments, const float* qlat_ts, const float* q0, float* q_final,
                         int n_ts);
 
+/* Diffusive-wave tridiagonal step (owp_extended_kernels.cu:24-91), float,
+ * arrays [n_reaches][max_nodes]. Returns 1 for an ncomp outside [1, max_nodes]. */
+typedef struct oracle_diff_reach {
+    int ncomp;
+    float theta;
+    float dtini;
+} oracle_diff_reach;
+int oracle_diffusive_tridiag(const oracle_diff_reach* rp, const float* dx, const float* diffusivity,
+                             const float* qp_prev, float* qp_out, int n_reaches, int max_nodes);
+
 #ifdef __cplusplus
 }
 #endif

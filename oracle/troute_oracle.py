@@ -73,6 +73,8 @@ def oracle():
         L.oracle_linear_coeffs.restype = None
         L.oracle_linear_route.argtypes = [_P] * 10 + [C.c_int] * 3 + [_P] * 3 + [C.c_int]
         L.oracle_linear_route.restype = C.c_int
+        L.oracle_diffusive_tridiag.argtypes = [_P] * 5 + [C.c_int, C.c_int]
+        L.oracle_diffusive_tridiag.restype = C.c_int
         L.oracle_set_pow_mode.argtypes = [C.c_int]
         L.oracle_set_pow_mode.restype = None
         L.oracle_pow23_53.argtypes = [C.c_double, _P, _P]
@@ -119,6 +121,9 @@ def ref():
         L.ref_linear_coeffs.restype = None
         L.ref_cpu_linear_mc.argtypes = [_P] * 10 + [C.c_int] * 3 + [_P] * 3 + [C.c_int]
         L.ref_cpu_linear_mc.restype = None
+        L.ref_cpu_diffusive_tridiag.argtypes = [_P] * 6 + [C.c_int]
+        L.ref_cpu_diffusive_tridiag.restype = None
+        L.ref_diffusive_max_nodes.restype = C.c_int
         _REF = L
     return _REF
 
@@ -336,4 +341,26 @@ def linear_route(coeffs, topo, qlat_ts, q0, level_ptr=None, level_reach=None, us
         rc = oracle().oracle_linear_route(*args)
         if rc:
             raise RuntimeError(f"oracle_linear_route failed: {rc}")
+    return out
+
+
+DIFF_REACH = np.dtype([("ncomp", "<i4"), ("theta", "<f4"), ("dtini", "<f4")])
+
+
+def diffusive_tridiag(reaches, dx, diffusivity, qp_prev, qp_out=None, use_ref=False, celerity=None):
+    """Diffusive-wave tridiagonal step over [n_reaches][max_nodes] arrays: the
+    oracle's restatement, or (use_ref) the reference's cpu_diffusive_tridiag
+    (whose arrays are [n][MAX_NODES = 500])."""
+    rp = np.ascontiguousarray(reaches, DIFF_REACH)
+    dx, df, qp = (np.ascontiguousarray(a, np.float32) for a in (dx, diffusivity, qp_prev))
+    n, m = qp.shape
+    out = np.zeros_like(qp) if qp_out is None else np.ascontiguousarray(qp_out, np.float32).copy()
+    if use_ref:
+        assert m == ref().ref_diffusive_max_nodes()
+        cel = np.zeros_like(qp) if celerity is None else np.ascontiguousarray(celerity, np.float32)
+        ref().ref_cpu_diffusive_tridiag(_ptr(rp), _ptr(dx), _ptr(df), _ptr(cel), _ptr(qp), _ptr(out), n)
+    else:
+        rc = oracle().oracle_diffusive_tridiag(_ptr(rp), _ptr(dx), _ptr(df), _ptr(qp), _ptr(out), n, m)
+        if rc:
+            raise RuntimeError(f"oracle_diffusive_tridiag failed: {rc}")
     return out
