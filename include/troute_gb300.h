@@ -389,6 +389,20 @@ void troute_free_network(troute_netfile* net);
 /* Writes the three files (byte-compatible with the reference's writer). */
 int troute_write_network(const char* dir, const troute_netfile* net);
 
+/* ---- lateral-inflow pre-processor -------------------------------------- */
+/* Pivots a directory of nex-<id>_output.csv files ("step, time, value" rows)
+ * into qlat[n_ts][n_reaches] (reach i takes the file whose id is
+ * reach_ids[i]; cells without a file stay 0), in parallel over files
+ * (n_threads <= 0: all hardware threads). The parsing rules of the reference's
+ * water-prediction/t-route/wavefront/data_parsers/parse_qlat_fast_cpp.cpp.
+ * matched / missing (optional): files used / files whose id is unknown. */
+int troute_qlat_from_csv(const char* csv_dir, const int64_t* reach_ids, int n_reaches, int n_ts, int n_threads,
+                         float* qlat, long long* matched, long long* missing);
+/* Writes forcings.bin: int32 n_ts, float32 qlat[n_ts][n_segments],
+ * qup0[n_reaches], qdp0[n_segments], dp0[n_segments]. */
+int troute_write_forcings(const char* path, int n_ts, int n_reaches, int n_segments, const float* qlat,
+                          const float* qup0, const float* qdp0, const float* dp0);
+
 /* ---- synthetic inputs (seeded, platform-independent) ------------------ */
 /* Uniform random binary river tree (Remy's algorithm) with n_leaves
  * headwaters -> 2*n_leaves-1 reaches, n_segments segments of 1..max_len per

@@ -163,6 +163,8 @@ _SIGS = {
     "troute_linear_destroy": ([_P], _I),
     "troute_linear_run_device": ([_P, _P, _I, _P, C.c_longlong, _P], _I),
     "troute_linear_route": ([_P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
+    "troute_qlat_from_csv": ([C.c_char_p, _P, _I, _I, _I, _P, _P, _P], _I),
+    "troute_write_forcings": ([C.c_char_p, _I, _I, _I, _P, _P, _P, _P], _I),
     "troute_read_network": ([C.c_char_p, _P], _I),
     "troute_free_network": ([_P], None),
     "troute_write_network": ([C.c_char_p, _P], _I),
@@ -657,6 +659,25 @@ class LinearNetwork:
 
     def __exit__(self, *a):
         self.close()
+
+
+def qlat_from_csv(csv_dir: str, reach_ids, n_ts: int, n_threads: int = 0):
+    """Parallel pivot of nex-<id>_output.csv files -> (qlat [n_ts][n_reaches]
+    float32, files matched, files missing)."""
+    ids = np.ascontiguousarray(reach_ids, np.int64)
+    out = np.zeros((n_ts, ids.size), np.float32)
+    m, x = C.c_longlong(), C.c_longlong()
+    _check(lib().troute_qlat_from_csv(os.fsencode(csv_dir), _ptr(ids), ids.size, int(n_ts), int(n_threads),
+                                      _ptr(out), C.byref(m), C.byref(x)))
+    return out, m.value, x.value
+
+
+def write_forcings(path: str, qlat, qup0, qdp0, dp0):
+    """forcings.bin writer (n_reaches from qup0, n_segments from qdp0)."""
+    ql = np.ascontiguousarray(qlat, np.float32)
+    a, b, c = (np.ascontiguousarray(v, np.float32) for v in (qup0, qdp0, dp0))
+    _check(lib().troute_write_forcings(os.fsencode(path), ql.shape[0], a.size, b.size, _ptr(ql), _ptr(a), _ptr(b),
+                                       _ptr(c)))
 
 
 WARM_NPARAMS = 4801

@@ -23,7 +23,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "route_pool.cu", "route_dataflow.cu", "noalloc.cu", "warm.cu", "linear.cu", "diffusive.cu"]
-CPP_SOURCES = ["network.cpp", "capi.cpp", "gen.cpp", "netfile.cpp"]
+CPP_SOURCES = ["network.cpp", "capi.cpp", "gen.cpp", "netfile.cpp", "forcing.cpp"]
 
 
 def _sources():
