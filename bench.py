@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--n-ts", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (profiling runs)")
     ap.add_argument("--warm", action="store_true",
                     help="learned warm start on a single-network workload (trained on its own plain-run pairs)")
     return ap.parse_args()
@@ -417,7 +418,7 @@ def run_ours(args, dist: Dist):
     qlat_dev = qlat_host.to(dev, non_blocking=False)
     levels = net.n_levels
     tune = None
-    if "batch" in w or "members" in w:
+    if ("batch" in w or "members" in w) and not args.no_tune:
         # the batched forms pick their launch shape with the autotuner (a trial of
         # half a bench step per candidate, from the same state; untimed)
         t0 = time.perf_counter()
@@ -518,7 +519,8 @@ def run_ours(args, dist: Dist):
             "gpu_launches": 4 * args.steps,
             "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
                        "early_exits": stats["early_exits"], "warm_used": stats["warm_used"],
-                       "warm_fallback_rate": stats["warm_fallback"] / max(1, stats["warm_used"])}}
+                       "warm_fallback_rate": stats["warm_fallback"] / max(1, stats["warm_used"]),
+                       "busy_lanes_per_warp_pass": stats["lane_busy"] / max(1, stats["warp_passes"])}}
     if tune:
         line["autotune"] = tune
     if model:
@@ -529,12 +531,50 @@ def run_ours(args, dist: Dist):
         print(json.dumps(line), flush=True)
 
 
+def run_linear(args, dist: Dist):
+    """lin:<network>: the linearised-MC approximate mode (FP32, one persistent
+    launch per run) on a single network; one bench step = one run of n_ts steps
+    from the carried-over discharge. Reported on its own metric line."""
+    import torch
+
+    import troute_gb300 as T
+
+    dev = torch.device("cuda", dist.local if dist.world > 1 else 0)
+    torch.cuda.set_device(dev)
+    w = workload(args.workload.split(":", 1)[1], args.n_ts)
+    S, n_ts = w["S"], w["qlat"].shape[0]
+    p32 = np.asarray(w["params"].view("<f8").reshape(-1, 8), np.float32)
+    coeffs = T.linear_coeffs(p32, w["dt"])
+    ql = torch.from_numpy(w["qlat"].astype(np.float32)).to(dev)
+    q = torch.from_numpy(w["q0"].astype(np.float32)).to(dev)
+    net = T.LinearNetwork(w["topo"], coeffs)
+    for _ in range(args.warmup):
+        net.run_device(ql.data_ptr(), n_ts, q.data_ptr())
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        net.run_device(ql.data_ptr(), n_ts, q.data_ptr())   # synchronous
+    el = dist.max(time.perf_counter() - t0)
+    net.close()
+    value = S * n_ts * args.steps * dist.world / el
+    if dist.rank == 0:
+        print(json.dumps({"metric": "segment-steps/s, linearised MC (approximate mode, FP32)", "value": value,
+                          "unit": UNIT, "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+                          "config": {"workload": f"{args.workload}: {S} segments, {n_ts} steps per bench step, "
+                                                 f"host-timed synchronous runs", "segments": S}}), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.workload.startswith("lin:"):
+            run_linear(args, dist)
         else:
             run_ours(args, dist)
     finally:
