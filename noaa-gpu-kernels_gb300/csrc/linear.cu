@@ -124,9 +124,20 @@ __global__ void __launch_bounds__(128) lin_dataflow_kernel(LinRun d)
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
+    // A lane holds at most one claimed queue slot. Claims are taken only for
+    // slots that are (or are about to be) written; a lane whose slot is not
+    // yet written keeps it and looks again in the next round, while the other
+    // lanes of its warp go on working -- a warp never blocks on one slot.
+    unsigned long long slot = 0;
+    bool holding = false;
+    long long t0 = 0;
+    unsigned long long seen = 0;
     unsigned sleep_ns = 64;
+    unsigned long long idle_seen = ~0ull;  // warp-uniform: n_done when this warp last saw progress
+    long long idle_t0 = clock64();
     while (true) {
-        // claim up to 32 queued items (warp-aggregated)
+        // ---- idle lanes claim queued slots (one atomic per warp) ----
+        const unsigned idle = __ballot_sync(kFull, !holding);
         unsigned n = 0;
         unsigned long long base = 0, nd = 0;
         int err = 0;
@@ -134,8 +145,8 @@ __global__ void __launch_bounds__(128) lin_dataflow_kernel(LinRun d)
             const unsigned long long tail = ld_vol_ull(d.rq_tail), head = ld_vol_ull(d.rq_head);
             nd = ld_vol_ull(d.n_done);
             err = *reinterpret_cast<volatile int*>(d.error);
-            if (tail > head && nd < d.n_items && !err) {
-                n = (unsigned)min(32ull, tail - head);
+            if (idle && tail > head && nd < d.n_items && !err) {
+                n = (unsigned)min((unsigned long long)__popc(idle), tail - head);
                 base = atomicAdd(d.rq_head, (unsigned long long)n);
             }
         }
@@ -143,49 +154,42 @@ __global__ void __launch_bounds__(128) lin_dataflow_kernel(LinRun d)
         base = __shfl_sync(kFull, base, 0);
         nd = __shfl_sync(kFull, nd, 0);
         err = __shfl_sync(kFull, err, 0);
+        // the run is over once every item has completed (claims past the last
+        // item are never written and are dropped)
         if (err || nd >= d.n_items) break;
-        if (n == 0) {
-            __nanosleep(sleep_ns);
-            sleep_ns = sleep_ns < 2048 ? 2 * sleep_ns : 2048;
-            continue;
+        if (!holding && n) {
+            const unsigned rank = __popc(idle & lt);
+            if (rank < n && base + rank < d.n_items) {
+                slot = base + rank;
+                holding = true;
+                t0 = clock64();
+                seen = nd;
+            }
         }
-        sleep_ns = 64;
-        // each claiming lane waits (bounded) for its slot to be written
-        const unsigned long long slot = base + lane;
-        bool have = lane < (int)n && slot < d.n_items;
+        // ---- lanes whose slot is written take the item ----
+        bool have = false;
         int r = -1, t = -1;
-        if (have) {
-            long long t0 = clock64();
-            unsigned long long seen = ld_vol_ull(d.n_done);
-            while (true) {
-                const long long v = *reinterpret_cast<const volatile long long*>(d.rq + slot);
-                if (v >= 0) {
-                    r = (int)(v & 0xffffffffll);
-                    t = (int)(v >> 32);
-                    break;
-                }
-                const unsigned long long now_done = ld_vol_ull(d.n_done);
-                if (now_done >= d.n_items || *reinterpret_cast<volatile int*>(d.error)) {
+        if (holding) {
+            const long long v = *reinterpret_cast<const volatile long long*>(d.rq + slot);
+            if (v >= 0) {
+                r = (int)(v & 0xffffffffll);
+                t = (int)(v >> 32);
+                holding = false;
+                have = true;
+                if (r < 0 || r >= d.R || t < 0 || t >= d.T) {
+                    atomicCAS(d.error, 0, TROUTE_EINVAL);  // an entry that names no item: never index with it
                     have = false;
-                    break;
                 }
-                if (clock64() - t0 > d.wait_cycles) {
-                    if (now_done == seen) {
-                        atomicCAS(d.error, 0, TROUTE_ETIMEOUT);
-                        have = false;
-                        break;
-                    }
-                    seen = now_done;
-                    t0 = clock64();
-                }
-                __nanosleep(32);
-            }
-            if (have && (r < 0 || r >= d.R || t < 0 || t >= d.T)) {
-                atomicCAS(d.error, 0, TROUTE_EINVAL);  // an entry that names no item: never index with it
-                have = false;
+            } else if (clock64() - t0 > d.wait_cycles) {
+                // a slot may stay empty for long while the run advances; give up
+                // only if no item completed during a whole wait budget
+                const unsigned long long now_done = ld_vol_ull(d.n_done);
+                if (now_done == seen) atomicCAS(d.error, 0, TROUTE_ETIMEOUT);
+                seen = now_done;
+                t0 = clock64();
             }
         }
-        // route the items, publish, count dependencies
+        // ---- route the items, publish, count dependencies ----
         int npush = 0;
         long long push0 = -1, push1 = -1;
         if (have) {
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(128) lin_dataflow_kernel(LinRun d)
             }
         }
         const unsigned done_mask = __ballot_sync(kFull, have);
-        // warp-aggregated append of the newly ready items
+        // ---- warp-aggregated append of the newly ready items ----
         unsigned total = npush;
         for (int off = 16; off > 0; off >>= 1) total += __shfl_xor_sync(kFull, total, off);
         if (total) {
@@ -229,7 +233,22 @@ __global__ void __launch_bounds__(128) lin_dataflow_kernel(LinRun d)
             if (npush >= 2) *reinterpret_cast<volatile long long*>(d.rq + pos + 1) = push1;
         }
         if (done_mask && lane == 0) atomicAdd(d.n_done, (unsigned long long)__popc(done_mask));
-        (void)lt;
+        // a warp that did nothing this round backs off before polling again;
+        // one that has seen no item complete anywhere for a whole wait budget
+        // reports a timeout (the run would otherwise never end)
+        if (done_mask == 0) {
+            if (nd != idle_seen) {
+                idle_seen = nd;
+                idle_t0 = clock64();
+            } else if (clock64() - idle_t0 > d.wait_cycles) {
+                if (lane == 0) atomicCAS(d.error, 0, TROUTE_ETIMEOUT);
+            }
+            __nanosleep(sleep_ns);
+            sleep_ns = sleep_ns < 2048 ? 2 * sleep_ns : 2048;
+        } else {
+            sleep_ns = 64;
+            idle_t0 = clock64();
+        }
     }
 }
 

@@ -173,6 +173,8 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
     L.mode = L_IDLE;
     unsigned long long n_pass = 0, n_busy = 0, n_wait = 0, n_idle = 0;
     unsigned idle_ns = kSleepMinNs;  // warp-uniform
+    unsigned long long idle_seen = ~0ull;  // warp-uniform: n_done when this warp last saw progress
+    long long idle_t0 = clock64();
 
     while (true) {
         // ---- idle lanes claim queue slots (one atomic per warp) ----
@@ -232,7 +234,19 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
         if (__ballot_sync(kFullMask, L.mode >= L_SOLVE) == 0) {
             unsigned long long nd = 0;
             if (lane == 0) nd = ld_volatile_ull(df.n_done);
-            if (__shfl_sync(kFullMask, nd, 0) >= df.n_items) break;
+            nd = __shfl_sync(kFullMask, nd, 0);
+            if (nd >= df.n_items) break;
+            // a warp without work that sees no item complete anywhere for a
+            // whole wait budget reports a timeout instead of polling forever
+            if (nd != idle_seen) {
+                idle_seen = nd;
+                idle_t0 = clock64();
+            } else if (clock64() - idle_t0 > run.wait_cycles) {
+                if (lane == 0) record_error(run.stats, TROUTE_ETIMEOUT, -1, -1, 10);
+                break;
+            }
+        } else {
+            idle_t0 = clock64();
         }
         {
             const unsigned wmask = __ballot_sync(kFullMask, L.mode == L_FETCH);

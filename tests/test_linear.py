@@ -75,8 +75,10 @@ def test_device_coefficients_within_float_rounding():
     c, p32, _, _ = synthetic()
     gd = T.linear_coeffs(p32)
     ho = O.linear_coeffs(p32)
+    # C1..C4/ql are at most ~1 in magnitude; C2 and C3 cancel (dt/2 - Km X)
+    # when Km is near dt, so the bound is absolute at that scale
     for a, b in zip(gd, ho):
-        assert np.all(np.abs(a - b) <= 4e-6 * np.maximum(np.abs(b), 1e-30))
+        assert np.all(np.abs(a - b) <= 4e-6 * np.maximum(np.abs(b), 1.0))
 
 
 @pytest.mark.gpu
