@@ -1,0 +1,105 @@
+// IEEE double comparisons, minimum and maximum evaluated on the integer
+// pipes from the bit patterns. On GB300 every FP64 instruction -- compares
+// and min/max included -- occupies an SMSP's FP64 pipe for 64 cycles per
+// warp, while the integer pipes are idle; the secant pass makes ~30 such
+// decisions. Each helper returns exactly what the IEEE comparison returns for
+// every input, NaN and signed zeros included (IEEE ordering of doubles is the
+// ordering of their sign-magnitude bit patterns, with NaN unordered and
+// +0 == -0).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace tr {
+
+constexpr long long kInfBits = 0x7ff0000000000000ll;
+
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
+// x > 0
+__device__ __forceinline__ bool fp_gt0(double x)
+{
+    const long long b = dbits(x);
+    return b > 0 && b <= kInfBits;
+}
+
+// x < 0
+__device__ __forceinline__ bool fp_lt0(double x)
+{
+    const unsigned long long b = (unsigned long long)dbits(x);
+    return b > 0x8000000000000000ull && b <= 0xfff0000000000000ull;
+}
+
+// x == 0 (either sign)
+__device__ __forceinline__ bool fp_eq0(double x) { return ((unsigned long long)dbits(x) << 1) == 0; }
+
+// x > c and x >= c for a constant or value c > 0 that is not NaN
+__device__ __forceinline__ bool fp_gt_pos(double x, double c)
+{
+    const long long b = dbits(x);
+    return b > dbits(c) && b <= kInfBits;
+}
+__device__ __forceinline__ bool fp_ge_pos(double x, double c)
+{
+    const long long b = dbits(x);
+    return b >= dbits(c) && b <= kInfBits;
+}
+
+// x >= c for c >= +0 (not NaN, not -0); x >= +0 is true for x = -0 as well
+__device__ __forceinline__ bool fp_ge_nonneg(double x, double c)
+{
+    const long long b = dbits(x);
+    if (((unsigned long long)b << 1) == 0) return dbits(c) == 0;  // x = +-0: only c = 0 qualifies
+    return b >= dbits(c) && b <= kInfBits;
+}
+
+// x < c for a constant or value c > 0 that is not NaN
+__device__ __forceinline__ bool fp_lt_pos(double x, double c)
+{
+    const long long b = dbits(x);
+    // sign set: -0 and negative numbers are below c, a negative NaN is not
+    return b < 0 ? (unsigned long long)b <= 0xfff0000000000000ull : b < dbits(c);
+}
+
+// |a| > b for any a, b (false when either is NaN)
+__device__ __forceinline__ bool fp_abs_gt(double a, double b)
+{
+    const long long ma = dbits(a) & 0x7fffffffffffffffll;
+    const long long bb = dbits(b);
+    const long long mb = bb & 0x7fffffffffffffffll;
+    if (ma > kInfBits || mb > kInfBits) return false;
+    if (bb < 0) return ma != 0 || mb != 0;  // b <= -0: |a| > b unless both are zeros
+    return ma > mb;
+}
+
+// fmax(x, 0.0) and fmax(0.0, x): the positive value, otherwise +0 (NaN -> +0,
+// as IEEE maxNum returns the non-NaN operand)
+__device__ __forceinline__ double fp_max0(double x) { return fp_gt0(x) ? x : 0.0; }
+
+// fmin(c, x) for c > 0 not NaN and x >= +0 or NaN (a NaN x gives c), and
+// fmax(c, x) for c > 0 not NaN and any x (x <= c or NaN gives c)
+__device__ __forceinline__ double fp_min_pos(double c, double x)
+{
+    const long long b = dbits(x);
+    return (b >= 0 && b < dbits(c)) ? x : c;
+}
+__device__ __forceinline__ double fp_max_pos(double c, double x) { return fp_gt_pos(x, c) ? x : c; }
+
+// 2.0 * a * b * c * d as the reference writes it, (((2a) b) c) d, given the
+// undoubled chain g1 = a b, g2 = g1 c, g = g2 d (all positive). Doubling
+// commutes with rounding while a product stays in the normal range, so when
+// g1, g2 and g are at least 2^-1021 and 2g is finite the result is exactly
+// 2g, formed by raising g's exponent on the integer pipe; otherwise it is
+// evaluated as written.
+__device__ __forceinline__ double twice_chain(double g1, double g2, double g, double a, double b, double c, double d)
+{
+    const unsigned e1 = (unsigned)((unsigned long long)dbits(g1) >> 52) & 0x7ffu;
+    const unsigned e2 = (unsigned)((unsigned long long)dbits(g2) >> 52) & 0x7ffu;
+    const unsigned e3 = (unsigned)((unsigned long long)dbits(g) >> 52) & 0x7ffu;
+    // exponents 2..0x7fd: the exact products are normal and their doubles finite
+    if (e1 - 2u < 0x7fcu && e2 - 2u < 0x7fcu && e3 - 2u < 0x7fcu)
+        return __longlong_as_double(dbits(g) + (1ll << 52));
+    return 2.0 * a * b * c * d;
+}
+
+}  // namespace tr

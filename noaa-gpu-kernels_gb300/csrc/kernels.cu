@@ -218,11 +218,11 @@ __global__ void velocity_kernel(NetDev net)
         double vel = 0.0;
         if (!(p.n_ch <= 0.0 || p.s0 <= 0.0 || p.z <= 0.0 || p.bw <= 0.0)) {
             const double h = __ldcg(net.d + s);
-            const double twl = p.bw + 2.0 * p.z * h;
+            const double twl = p.bw + p.z2 * h;
             double Rv = (h * (p.bw + twl) / 2.0) /
                         (p.bw + 2.0 * sqrt(((twl - p.bw) / 2.0) * ((twl - p.bw) / 2.0) + h * h));
             if (Rv < 0.0) Rv = 0.0;
-            vel = p.inv_n * pow23(Rv) * p.sq_s0;
+            vel = (1.0 / p.n_ch) * pow23(Rv) * p.sq_s0;
         }
         __stcg(net.v + s, vel);
     }

@@ -18,6 +18,7 @@
 #pragma once
 
 #include "device_common.cuh"
+#include "fpbits.cuh"
 
 namespace tr {
 
@@ -110,63 +111,76 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
         // the segment's parameters are re-read (L1) every pass rather than held
         // in registers across the kernel's scheduling code
         const SegP p = load_seg(net, L.s);
-        const double x = L.need0 ? L.h_0 : L.h;
-        const double twl = p.bw + 2.0 * p.z * x;
-        double above = fmax(x - p.bfd, 0.0);
-        double below = fmin(p.bfd, x);
-        if (above > 0.0 && p.twcc <= 0.0) {
+        const double x = L.need0 ? L.h_0 : L.h;  // >= +0
+        // Every comparison, minimum and maximum of the pass runs on the integer
+        // pipes (fpbits.cuh: the IEEE results, bit for bit), leaving the FP64
+        // pipe to the arithmetic.
+        const bool twcc_pos = fp_gt0(p.twcc);
+        const double twl = p.bw + p.z2 * x;  // bw + 2 z x
+        double above = fp_max0(x - p.bfd);
+        double below = fp_min_pos(p.bfd, x);
+        if (fp_gt0(above) && (fp_lt0(p.twcc) || fp_eq0(p.twcc))) {
             above = 0.0;
             below = x;
         }
         const double A = (p.bw + below * p.z) * below;
-        const double WP = p.bw + 2.0 * below * p.sq_1z2;
+        const double WP = p.bw + below * p.sq2;  // bw + 2 below sqrt(1+z^2)
         const double AC = p.twcc * above;
-        const double WPC = (above > 0.0) ? (p.twcc + 2.0 * above) : 0.0;
+        const double WPC = fp_gt0(above) ? (p.twcc + 2.0 * above) : 0.0;
         const double P = WP + WPC;
-        const double R = (P > 0.0) ? (A + AC) / P : 0.0;
+        const bool P_pos = fp_gt0(P);
+        const double R = P_pos ? (A + AC) / P : 0.0;
         double r23, r53;
         pow23_53(R, &r23, &r53);
         {
             DepthEval e;
             e.Ck = 0.0;
-            if (x > 0.0)
-                e.Ck = fmax(0.0, p.ck_fac * ((5.0 / 3.0) * r23 -
-                                             (2.0 / 3.0) * r53 * (2.0 * p.sq_1z2 / (p.bw + 2.0 * x * p.z))));
-            e.Km = (e.Ck > 0.0) ? fmax(dt, p.dx / e.Ck) : dt;
-            e.twu = (x > p.bfd && p.twcc > 0.0) ? p.twcc : twl;
-            e.Qmn = (P > 0.0) ? (1.0 / ((WP * p.n_ch + WPC * p.ncc) / P)) * (A + AC) * r23 * p.sq_s0 : 0.0;
+            // 2 sqrt(1+z^2) / (bw + 2 x z): the denominator is twl
+            if (fp_gt0(x)) e.Ck = fp_max0(p.ck_fac * ((5.0 / 3.0) * r23 - (2.0 / 3.0) * r53 * (p.sq2 / twl)));
+            e.Km = fp_gt0(e.Ck) ? fp_max_pos(dt, p.dx / e.Ck) : dt;
+            e.twu = (fp_gt_pos(x, p.bfd) && twcc_pos) ? p.twcc : twl;
+            e.Qmn = P_pos ? (1.0 / ((WP * p.n_ch + WPC * p.ncc) / P)) * (A + AC) * r23 * p.sq_s0 : 0.0;
             if (L.need0) {
                 L.e0 = e;
                 L.need0 = 0;
             } else {
                 const double qup = L.qup, quc = L.quc, qdp = L.qdp, ql = L.ql;
                 const DepthEval& e0 = L.e0;
-                const double X0 = (e0.Ck > 0.0 && e0.twu * p.s0 * e0.Ck * p.dx > 0.0)
-                                      ? fmin(0.5, fmax(0.0, 0.5 * (1.0 - L.Qj_0 / (2.0 * e0.twu * p.s0 * e0.Ck * p.dx))))
-                                      : 0.5;
+                // X at the lower depth, clamped to [0, 0.5] (troute_mc_final.cu:86)
+                double X0 = 0.5;
+                {
+                    const double g1 = e0.twu * p.s0, g2 = g1 * e0.Ck, g = g2 * p.dx;
+                    if (fp_gt0(e0.Ck) && fp_gt0(g))
+                        X0 = fp_min_pos(0.5, fp_max0(0.5 * (1.0 - L.Qj_0 / twice_chain(g1, g2, g, e0.twu, p.s0, e0.Ck, p.dx))));
+                }
                 double D0 = e0.Km * (1.0 - X0) + dt / 2.0;
-                if (D0 == 0.0) D0 = 1.0;
+                if (fp_eq0(D0)) D0 = 1.0;
                 const double c1 = (e0.Km * X0 + dt / 2.0) / D0;
                 const double c2 = (dt / 2.0 - e0.Km * X0) / D0;
                 const double c3 = (e0.Km * (1.0 - X0) - dt / 2.0) / D0;
                 const double c4 = (ql * dt) / D0;
                 const double qmc0 = c1 * qup + c2 * quc + c3 * qdp + c4;
                 L.Qj_0 = qmc0 - e0.Qmn;
-                const double X = (e.Ck > 0.0 && e.twu * p.s0 * e.Ck * p.dx > 0.0)
-                                     ? fmin(0.5, fmax(0.25, 0.5 * (1.0 - qmc0 / (2.0 * e.twu * p.s0 * e.Ck * p.dx))))
-                                     : 0.5;
+                // X at the upper depth, clamped to [0.25, 0.5] (troute_mc_final.cu:105)
+                double X = 0.5;
+                {
+                    const double g1 = e.twu * p.s0, g2 = g1 * e.Ck, g = g2 * p.dx;
+                    if (fp_gt0(e.Ck) && fp_gt0(g))
+                        X = fp_min_pos(0.5, fp_max_pos(0.25, 0.5 * (1.0 - qmc0 / twice_chain(g1, g2, g, e.twu, p.s0, e.Ck, p.dx))));
+                }
                 double D1 = e.Km * (1.0 - X) + dt / 2.0;
-                if (D1 == 0.0) D1 = 1.0;
+                if (fp_eq0(D1)) D1 = 1.0;
                 const double C1 = (e.Km * X + dt / 2.0) / D1;
                 const double C2 = (dt / 2.0 - e.Km * X) / D1;
                 const double C3 = (e.Km * (1.0 - X) - dt / 2.0) / D1;
                 double C4 = (ql * dt) / D1;
-                if (C4 < 0.0 && fabs(C4) > C1 * qup + C2 * quc + C3 * qdp) C4 = -(C1 * qup + C2 * quc + C3 * qdp);
-                const double Qj = (C1 * qup + C2 * quc + C3 * qdp + C4) - e.Qmn;
+                const double S3 = C1 * qup + C2 * quc + C3 * qdp;
+                if (fp_lt0(C4) && fp_abs_gt(C4, S3)) C4 = -S3;
+                const double Qj = (S3 + C4) - e.Qmn;
                 // outflow of the last evaluated coefficients (troute_mc_final.cu:125-130)
-                const double Qmc = C1 * qup + C2 * quc + C3 * qdp + C4;
-                if (Qmc < 0.0) {
-                    if (C4 < 0.0 && fabs(C4) > C1 * qup + C2 * quc + C3 * qdp)
+                const double Qmc = S3 + C4;
+                if (fp_lt0(Qmc)) {
+                    if (fp_lt0(C4) && fp_abs_gt(C4, S3))
                         L.qdc = 0.0;
                     else
                         L.qdc = fmax(C1 * qup + C2 * quc + C4, C1 * qup + C3 * qdp + C4);
@@ -174,35 +188,37 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                     L.qdc = Qmc;
                 }
                 const double h = L.h;
-                double h_1 = (L.Qj_0 - Qj != 0.0) ? h - (Qj * (L.h_0 - h)) / (L.Qj_0 - Qj) : h;
-                if (h_1 < 0.0) h_1 = h;
+                const double dQ = L.Qj_0 - Qj;
+                double h_1 = !fp_eq0(dQ) ? h - (Qj * (L.h_0 - h)) / dQ : h;
+                if (fp_lt0(h_1)) h_1 = h;
                 double rerr, aerr;
-                if (h > 0.0) {
+                if (fp_gt0(h)) {
                     rerr = fabs((h_1 - h) / h);
                     aerr = fabs(h_1 - h);
                 } else {
                     rerr = 0.0;
                     aerr = 0.9;
                 }
-                L.h_0 = fmax(0.0, h);
-                L.h = fmax(0.0, h_1);
+                L.h_0 = fp_max0(h);
+                L.h = fp_max0(h_1);
                 L.e0 = e;
                 ++L.iter;
                 ++L.total;
+                const bool more = fp_gt_pos(rerr, tol.rtol) && fp_ge_nonneg(aerr, tol.atol);
                 bool stop;
                 if (L.warm == W_ACTIVE) {
                     // warm phase: accepted once the stop test passes at a depth of at
                     // least kMinDepth; otherwise, after warm_k passes (or below
                     // kMinDepth), the plain solve restarts from the previous depth
-                    const bool conv = !(rerr > tol.rtol && aerr >= tol.atol);
-                    stop = conv && L.h >= kMinDepth;
-                    if (!stop && (L.h < kMinDepth || L.iter >= run.warm_k)) {
+                    const bool below_min = fp_lt_pos(L.h, kMinDepth);
+                    stop = !more && !below_min;
+                    if (!stop && (below_min || L.iter >= run.warm_k)) {
                         L.warm = W_PLAIN;
                         ls.warm_fallback++;
                         plain_bracket(L, tol);
                     }
                 } else {
-                    stop = (L.h < kMinDepth) || !(rerr > tol.rtol && aerr >= tol.atol && L.iter <= L.maxiter);
+                    stop = fp_lt_pos(L.h, kMinDepth) || !(more && L.iter <= L.maxiter);
                 }
                 if (stop) {
                     bool done = true;

@@ -33,7 +33,7 @@ __device__ __forceinline__ SegP load_seg(const NetDev& net, long long s)
     const double2 e = __ldg(net.prm[3] + s), f = __ldg(net.prm[4] + s), g = __ldg(net.prm[5] + s);
     SegP p;
     p.dx = a.x; p.bw = a.y; p.twcc = b.x; p.n_ch = b.y; p.ncc = c.x; p.s0 = c.y;
-    p.z = e.x; p.bfd = e.y; p.sq_s0 = f.x; p.sq_1z2 = f.y; p.ck_fac = g.x; p.inv_n = g.y;
+    p.z = e.x; p.bfd = e.y; p.sq_s0 = f.x; p.sq2 = f.y; p.ck_fac = g.x; p.z2 = g.y;
     return p;
 }
 
@@ -45,7 +45,7 @@ struct DepthEval {
 
 __device__ __forceinline__ DepthEval eval_depth(double h, const SegP& p, double dt)
 {
-    const double twl = p.bw + 2.0 * p.z * h;
+    const double twl = p.bw + p.z2 * h;  // bw + 2 z h
     double above = fmax(h - p.bfd, 0.0);
     double below = fmin(p.bfd, h);
     if (above > 0.0 && p.twcc <= 0.0) {
@@ -53,7 +53,7 @@ __device__ __forceinline__ DepthEval eval_depth(double h, const SegP& p, double 
         below = h;
     }
     const double A = (p.bw + below * p.z) * below;
-    const double WP = p.bw + 2.0 * below * p.sq_1z2;
+    const double WP = p.bw + below * p.sq2;  // bw + 2 below sqrt(1+z^2)
     const double AC = p.twcc * above;
     const double WPC = (above > 0.0) ? (p.twcc + 2.0 * above) : 0.0;
     const double P = WP + WPC;
@@ -63,8 +63,8 @@ __device__ __forceinline__ DepthEval eval_depth(double h, const SegP& p, double 
     DepthEval e;
     e.Ck = 0.0;
     if (h > 0.0) {
-        e.Ck = fmax(0.0, p.ck_fac * ((5.0 / 3.0) * r23 -
-                                     (2.0 / 3.0) * r53 * (2.0 * p.sq_1z2 / (p.bw + 2.0 * h * p.z))));
+        // 2 sqrt(1+z^2) / (bw + 2 h z), the denominator being twl
+        e.Ck = fmax(0.0, p.ck_fac * ((5.0 / 3.0) * r23 - (2.0 / 3.0) * r53 * (p.sq2 / twl)));
     }
     e.Km = (e.Ck > 0.0) ? fmax(dt, p.dx / e.Ck) : dt;
     e.twu = (h > p.bfd && p.twcc > 0.0) ? p.twcc : twl;
@@ -174,12 +174,12 @@ __device__ __forceinline__ SolveOut mc_solve(double dt, double qup, double quc, 
     } else {
         qdc = Qmc;
     }
-    const double twl = p.bw + 2.0 * p.z * h;
+    const double twl = p.bw + p.z2 * h;
     double Rv = (h * (p.bw + twl) / 2.0) /
                 (p.bw + 2.0 * sqrt(((twl - p.bw) / 2.0) * ((twl - p.bw) / 2.0) + h * h));
     if (Rv < 0.0) Rv = 0.0;
     o.q = qdc;
-    o.vel = p.inv_n * pow23(Rv) * p.sq_s0;
+    o.vel = (1.0 / p.n_ch) * pow23(Rv) * p.sq_s0;
     o.depth = h;
     o.iters = total;
     return o;

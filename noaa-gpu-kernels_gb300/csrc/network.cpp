@@ -73,7 +73,9 @@ int check_cfg(const troute_cfg& c)
     return TROUTE_OK;
 }
 
-Tol make_tol(const troute_cfg& c) { return Tol{c.rtol, c.atol, c.maxiter, c.attempts}; }
+// atol + 0.0 turns a -0 tolerance into +0 (the same stop test; the device's
+// integer-pipe comparison expects a non-negative tolerance of either sign bit 0)
+Tol make_tol(const troute_cfg& c) { return Tol{c.rtol, c.atol + 0.0, c.maxiter, c.attempts}; }
 
 int cuda_check(cudaError_t e, const char* what)
 {
@@ -304,8 +306,8 @@ static void put_params(Layout& Lt, long long t, const troute_chparams& c)
     Lt.planes[1][t] = double2{p.twcc, p.n_ch};
     Lt.planes[2][t] = double2{p.ncc, p.s0};
     Lt.planes[3][t] = double2{p.z, p.bfd};
-    Lt.planes[4][t] = double2{p.sq_s0, p.sq_1z2};
-    Lt.planes[5][t] = double2{p.ck_fac, p.inv_n};
+    Lt.planes[4][t] = double2{p.sq_s0, p.sq2};
+    Lt.planes[5][t] = double2{p.ck_fac, p.z2};
 }
 
 // Schedule and layout of a forest (ALAP levels, level-blocks, tiles).

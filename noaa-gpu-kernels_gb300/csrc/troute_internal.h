@@ -41,12 +41,15 @@ struct Tol {
 // with the same IEEE operations the reference performs per solve
 // (troute_mc_final.cu:181-183), stored as six double2 planes.
 //   p[0] = {dx, bw}        p[1] = {twcc, n_ch}      p[2] = {ncc, s0}
-//   p[3] = {z, bfd}        p[4] = {sqrt(s0), sqrt(1+z^2)}
-//   p[5] = {sqrt(s0)/n_ch, 1/n_ch}
+//   p[3] = {z, bfd}        p[4] = {sqrt(s0), 2 sqrt(1+z^2)}
+//   p[5] = {sqrt(s0)/n_ch, 2 z}
+// The doubled values are exact (scaling by 2), and the reference's products
+// 2.0 * z * h and 2.0 * below * sqrt(1+z^2) round to the same double as
+// (2z) * h and below * (2 sqrt(1+z^2)): doubling commutes with rounding.
 constexpr int kParamPlanes = 6;
 
 struct SegP {
-    double dx, bw, twcc, n_ch, ncc, s0, z, bfd, sq_s0, sq_1z2, ck_fac, inv_n;
+    double dx, bw, twcc, n_ch, ncc, s0, z, bfd, sq_s0, sq2, ck_fac, z2;
 };
 
 // Derived values from the reference's parameter record, :181-183.
@@ -57,9 +60,9 @@ TR_HD inline SegP derive_seg(const troute_chparams& c)
     p.z = (c.cs == 0.0) ? 1.0 : 1.0 / c.cs;
     p.bfd = (c.bw > c.tw) ? c.bw / 0.00001 : (c.bw == c.tw) ? c.bw / (2.0 * p.z) : (c.tw - c.bw) / (2.0 * p.z);
     p.sq_s0 = sqrt(c.s0);
-    p.sq_1z2 = sqrt(1.0 + p.z * p.z);
+    p.sq2 = 2.0 * sqrt(1.0 + p.z * p.z);
     p.ck_fac = p.sq_s0 / c.n_ch;
-    p.inv_n = 1.0 / c.n_ch;
+    p.z2 = 2.0 * p.z;
     return p;
 }
 
