@@ -10,8 +10,8 @@ Default workload c4w (the combined form): a 64-member ensemble over the
 inflow x LogN(0, 0.3) and Manning's n x U(0.8, 1.2) per member -- routed in one
 persistent launch with the learned warm start, FP64 state. The MLP is trained
 in the same run, untimed, on (input, converged depth) pairs of an 18-step
-plain run of the single network (~49M pairs). One bench "step" = 8 routed
-time steps of all 64 members (1.4G segment-steps), replayed from a captured
+plain run of the single network (~49M pairs). One bench "step" = 16 routed
+time steps of all 64 members (2.8G segment-steps), replayed from a captured
 CUDA graph, the state carrying over. Beside it, in the same run, the plain
 single-basin routing of the same network (144 steps per graph launch) is
 timed: `plain_single_basin`, and `speedup_vs_plain` = value / that.
@@ -190,7 +190,7 @@ def workload(name: str, n_ts: int | None, all_members: bool = True):
     """Single networks ('c1', 'c0', 'tree:<segments>', 'c3' = fresh-seed c1
     with warm start) or the batched forms: 'c2' (256 basins with
     LogU(500, 200,000) segments, 288 steps), 'c4' / 'c4w' (64 ensemble
-    members of the c1 network, without / with warm start; 8 steps per bench
+    members of the c1 network, without / with warm start; 16 steps per bench
     step)."""
     from troute_gb300 import synth
 
@@ -213,7 +213,7 @@ def workload(name: str, n_ts: int | None, all_members: bool = True):
             M, base_net = int(parts[1]), f"tree:{int(parts[2])}"
         else:
             M, base_net = 64, "c1"
-        T = 8 if n_ts is None else n_ts
+        T = 16 if n_ts is None else n_ts
         w = synth.network(base_net, n_ts=T)
         w["base"] = base_net
         S = w["topo"]["n_segments"]
@@ -422,9 +422,10 @@ def run_ours(args, dist: Dist):
         # the batched forms pick their launch shape with the autotuner (a trial of
         # half a bench step per candidate, from the same state; untimed)
         t0 = time.perf_counter()
-        tune = net.autotune(qlat_dev.data_ptr(), max(1, n_ts // 2), repeats=1, all_mappings=not model)
+        trial = max(1, n_ts // 4)
+        tune = net.autotune(qlat_dev.data_ptr(), trial, repeats=1, all_mappings=not model)
         tune["tune_s"] = round(time.perf_counter() - t0, 2)
-        tune["trial_steps"] = max(1, n_ts // 2)
+        tune["trial_steps"] = trial
     net.graph_capture(qlat_dev.data_ptr(), n_ts)
     for _ in range(args.warmup):
         net.graph_launch(stream.cuda_stream)
