@@ -872,6 +872,8 @@ static int enqueue_chunk(troute_handle* H, const double* qlat_dev, int n_ts, con
     run.warm = H->cfg.warm_start ? 1 : 0;
     run.warm_k = H->cfg.warm_k;
     run.warm_delta = H->warm_delta;
+    run.warm_hi = 1.0 + H->warm_delta;
+    run.warm_lo = 1.0 - H->warm_delta;
     if ((rc = cuda_check(cudaMemsetAsync(H->ticket.p, 0, sizeof(unsigned long long), st), "memset"))) return rc;
     if (H->mapping == 3) {
         DataflowDev df;

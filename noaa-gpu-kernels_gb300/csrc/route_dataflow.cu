@@ -114,24 +114,28 @@ __device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const W
     if (!__any_sync(0xffffffffu, pend)) return;
     float f[kWIn];
     if (pend) {
-        f[0] = warm_feature(L.qup, true, m.mu[0], m.sd[0]);
-        f[1] = warm_feature(L.quc, true, m.mu[1], m.sd[1]);
-        f[2] = warm_feature(L.qdp, true, m.mu[2], m.sd[2]);
-        f[3] = warm_feature(L.ql, true, m.mu[3], m.sd[3]);
+        // features on the FP32 / integer pipes: truncating double -> float
+        f[0] = warm_feature(pos_to_float(L.qup), true, m.mu[0], m.inv_sd[0]);
+        f[1] = warm_feature(pos_to_float(L.quc), true, m.mu[1], m.inv_sd[1]);
+        f[2] = warm_feature(pos_to_float(L.qdp), true, m.mu[2], m.inv_sd[2]);
+        f[3] = warm_feature(pos_to_float(L.ql), true, m.mu[3], m.inv_sd[3]);
         const double2 p0 = __ldg(net.prm[0] + L.s), p1 = __ldg(net.prm[1] + L.s), p2 = __ldg(net.prm[2] + L.s);
-        f[4] = warm_feature(p0.x, false, m.mu[4], m.sd[4]);   // dx
-        f[5] = warm_feature(p2.y, false, m.mu[5], m.sd[5]);   // s0
-        f[6] = warm_feature(p1.y, false, m.mu[6], m.sd[6]);   // n
-        f[7] = warm_feature(p0.y, false, m.mu[7], m.sd[7]);   // bw
+        f[4] = warm_feature(pos_to_float(p0.x), false, m.mu[4], m.inv_sd[4]);   // dx
+        f[5] = warm_feature(pos_to_float(p2.y), false, m.mu[5], m.inv_sd[5]);   // s0
+        f[6] = warm_feature(pos_to_float(p1.y), false, m.mu[6], m.inv_sd[6]);   // n
+        f[7] = warm_feature(pos_to_float(p0.y), false, m.mu[7], m.inv_sd[7]);   // bw
     } else {
         for (int k = 0; k < kWIn; ++k) f[k] = 0.0f;
     }
     const float y = warm_mlp_warp(s, f, pend, m.b3);
     if (pend) {
-        const double pr = (double)expf(y * m.sd_y + m.mu_y);
-        if (pr > 0.0 && pr < 1.0e4) {
-            L.h = pr * (1.0 + run.warm_delta);
-            L.h_0 = pr * (1.0 - run.warm_delta);
+        const float prf = __expf(y * m.sd_y + m.mu_y);
+        const unsigned pb = __float_as_uint(prf);
+        // a normal positive float below 1e4 m (0x461c4000), else the plain bracket
+        if (pb >= 0x00800000u && pb < 0x461c4000u) {
+            const double pr = widen_pos(prf);
+            L.h = pr * run.warm_hi;   // 1 + delta
+            L.h_0 = pr * run.warm_lo; // 1 - delta
             L.warm = W_ACTIVE;
             ls.warm_used++;
             if (run.start_hist) __stcg(run.start_hist + (size_t)L.tau * (size_t)net.n_seg_int + L.s, pr);

@@ -121,6 +121,7 @@ struct RunDev {
     int warm;                // 1: solves start from the learned depth (dataflow kernel only)
     int warm_k;              // passes of the warm phase before the plain fallback
     double warm_delta;       // relative half-width of the warm bracket
+    double warm_hi, warm_lo; // 1 + warm_delta, 1 - warm_delta
 };
 
 // Ready-queue state of one run of the dataflow kernel (mapping 3).

@@ -244,8 +244,8 @@ __global__ void __launch_bounds__(128) warm_predict_kernel(WarmDev m, const floa
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float f[kWIn];
     for (int k = 0; k < kWIn; ++k) {
-        const double v = (i < n) ? (double)raw[(size_t)i * kWIn + k] : 1.0;
-        f[k] = warm_feature(v, k < 4, m.mu[k], m.sd[k]);
+        const float v = (i < n) ? raw[(size_t)i * kWIn + k] : 1.0f;
+        f[k] = warm_feature(v, k < 4, m.mu[k], m.inv_sd[k]);
     }
     const float yh = warm_mlp_warp(s, f, i < n, m.b3);
     if (i < n) depth[i] = (double)__expf(yh * m.sd_y + m.mu_y);
@@ -440,6 +440,7 @@ WarmDev warm_device_view(const troute_warm* w, double delta, int k)
     for (int i = 0; i < kWIn; ++i) {
         m.mu[i] = w->nm.mu[i];
         m.sd[i] = w->nm.sd[i];
+        m.inv_sd[i] = 1.0f / w->nm.sd[i];
     }
     m.mu_y = w->nm.mu_y;
     m.sd_y = w->nm.sd_y;

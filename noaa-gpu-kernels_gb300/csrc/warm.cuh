@@ -29,7 +29,7 @@ struct WarmDev {
     const float* b1;           // [64]
     const float* b2;           // [64]
     float b3;
-    float mu[kWIn], sd[kWIn];
+    float mu[kWIn], sd[kWIn], inv_sd[kWIn];
     float mu_y, sd_y;
     double delta;              // half-width of the starting bracket around the prediction (relative)
     int k;                     // iterations a warm-started solve gets before the plain restart
@@ -58,10 +58,34 @@ __device__ __forceinline__ void warm_stage(WarmSmem& s, const WarmDev& m)
     }
 }
 
-__device__ __forceinline__ float warm_feature(double v, bool flow, float mu, float sd)
+// A positive double as a float, truncated, on the integer pipe (the FP64
+// pipe, shared with the secant's arithmetic, is kept free): exponent rebias
+// and the top 23 mantissa bits. Non-positive values give 0, values outside
+// float's normal range are clamped to it. The features only need a
+// deterministic monotone map, not correct rounding.
+__device__ __forceinline__ float pos_to_float(double v)
 {
-    const float x = flow ? (float)v + kFlowFloor : (float)v;
-    return (__logf(fmaxf(x, 1e-30f)) - mu) / sd;
+    const long long b = __double_as_longlong(v);
+    if (b <= 0) return 0.0f;
+    const int e = (int)(b >> 52);  // biased exponent; the sign bit is 0
+    if (e > 1150) return 3.4e38f;
+    if (e < 897) return 1.18e-38f;
+    return __int_as_float(((e - 896) << 23) | (int)((b >> 29) & 0x7fffff));
+}
+
+// A positive normal float as the equal double, on the integer pipe.
+__device__ __forceinline__ double widen_pos(float f)
+{
+    const unsigned fb = __float_as_uint(f);
+    return __longlong_as_double(((long long)((fb >> 23) + 896) << 52) | ((long long)(fb & 0x7fffff) << 29));
+}
+
+// Raw input -> feature: log of the value (flows offset by kFlowFloor m3/s, which
+// may be zero), standardised with the training set's mean / standard deviation.
+__device__ __forceinline__ float warm_feature(float x, bool flow, float mu, float inv_sd)
+{
+    if (flow) x += kFlowFloor;
+    return (__logf(fmaxf(x, 1e-30f)) - mu) * inv_sd;
 }
 
 __device__ __forceinline__ unsigned int pack_bf16(float lo, float hi)
