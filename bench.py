@@ -174,16 +174,18 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profiled_traffic_per_seg_step():
-    """DRAM bytes per segment-step of route_kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "route_kernel_c1.md")
+def profiled(key: str, warm: bool):
+    """A figure of the routing kernel from the committed ncu summary: the
+    warm-started kernel's (an ensemble capture) or the plain kernel's."""
+    name = "route_dataflow_warm_ens64.md" if warm else "route_kernel_c1.md"
+    p = os.path.join(ROOT, "profiles", name)
     try:
         for ln in open(p):
-            if ln.strip().startswith("dram_bytes_per_seg_step:"):
-                return float(ln.split(":")[1])
+            if ln.strip().startswith(key + ":"):
+                return float(ln.split(":")[1]), name
     except OSError:
         pass
-    return None
+    return None, name
 
 
 def workload(name: str, n_ts: int | None, all_members: bool = True):
@@ -464,11 +466,14 @@ def run_ours(args, dist: Dist):
     peak, peak_kind = measured_peak_hbm()
     alg_bytes = BYTES_PER_SEG_STEP * seg_steps
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
-    tr = profiled_traffic_per_seg_step()
+    tr, tr_src = profiled("dram_bytes_per_seg_step", bool(model))
+    fp64, _ = profiled("fp64_pipe_active_pct", bool(model))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": (tr * seg_steps if tr is not None else None),
+                "traffic_source": f"profiles/{tr_src} (DRAM bytes per segment-step x segment-steps of a launch)",
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                "note": "the secant loop is FP64-pipe bound; DRAM traffic is far below the HBM roofline"}
+                "fp64_pipe_active_pct": fp64,
+                "note": "the secant loop is FP64-pipe and dependency bound; DRAM traffic is far below the HBM roofline"}
 
     e2e = None
     if not args.no_e2e:

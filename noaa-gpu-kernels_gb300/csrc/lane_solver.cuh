@@ -23,6 +23,30 @@
 namespace tr {
 
 enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_DONE = 4 };
+
+// A lane's current segment parameters live in shared memory for the whole
+// solve: copied once when the solve starts, read by every pass. (Re-reading
+// them from global memory every pass misses L2 once a network's parameters
+// outgrow it -- c1's are 260 MB -- and costs a DRAM round trip per pass.)
+// Layout [plane][thread of the block]: a warp's reads of one plane are 512
+// contiguous bytes, free of bank conflicts.
+constexpr int kSegSmemStride = 128;  // threads per block of the per-lane kernels
+
+__device__ __forceinline__ void stage_seg(const NetDev& net, long long s, double2* slot)
+{
+#pragma unroll
+    for (int k = 0; k < kParamPlanes; ++k) slot[k * kSegSmemStride] = __ldg(net.prm[k] + s);
+}
+
+__device__ __forceinline__ SegP staged_seg(const double2* slot)
+{
+    const double2 a = slot[0], b = slot[kSegSmemStride], c = slot[2 * kSegSmemStride];
+    const double2 e = slot[3 * kSegSmemStride], f = slot[4 * kSegSmemStride], g = slot[5 * kSegSmemStride];
+    SegP p;
+    p.dx = a.x; p.bw = a.y; p.twcc = b.x; p.n_ch = b.y; p.ncc = c.x; p.s0 = c.y;
+    p.z = e.x; p.bfd = e.y; p.sq_s0 = f.x; p.sq2 = f.y; p.ck_fac = g.x; p.z2 = g.y;
+    return p;
+}
 // Warm-start phase of a solve: plain bracket, waiting for the learned depth
 // (set by the kernel before the next pass), or bracketing the learned depth.
 enum : int { W_PLAIN = 0, W_PENDING = 1, W_ACTIVE = 2 };
@@ -62,7 +86,7 @@ __device__ __forceinline__ void plain_bracket(Lane& L, const Tol& tol)
 // right away. Returns true when a secant solve is pending, false when the reach
 // is complete.
 __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const RunDev& run,
-                                              LocalStats& ls, unsigned int* hist_s)
+                                              LocalStats& ls, unsigned int* hist_s, double2* slot)
 {
     const double* qlat_row = run.qlat + (size_t)L.tau * (size_t)run.qlat_ld;
     while (L.i < L.ns) {
@@ -71,7 +95,8 @@ __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const 
         const double dpp = __ldcg(net.d + L.s);
         L.ql = __ldg(qlat_row + __ldg(net.qcol + L.s));
         if (net.qscale) L.ql *= __ldg(net.qscale + L.s);
-        const SegP p = load_seg(net, L.s);
+        stage_seg(net, L.s, slot);
+        const SegP p = staged_seg(slot);
         L.qup = (L.i == 0) ? L.qup_head : L.q_up_old;
         L.quc = (L.i == 0) ? L.quc_head : L.q_up_new;
         if (p.n_ch <= 0.0 || p.s0 <= 0.0 || p.z <= 0.0 || p.bw <= 0.0 ||
@@ -103,14 +128,13 @@ __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const 
 
 // One evaluation pass of a lane in SOLVE or VEL mode (no-op otherwise).
 __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunDev& run, LocalStats& ls,
-                                          unsigned int* hist_s)
+                                          unsigned int* hist_s, double2* slot)
 {
     const Tol& tol = run.tol;
     const double dt = run.dt;
     if (L.mode == L_SOLVE && L.warm != W_PENDING) {
-        // the segment's parameters are re-read (L1) every pass rather than held
-        // in registers across the kernel's scheduling code
-        const SegP p = load_seg(net, L.s);
+        // the segment's parameters, staged in shared memory when the solve began
+        const SegP p = staged_seg(slot);
         const double x = L.need0 ? L.h_0 : L.h;  // >= +0
         // Every comparison, minimum and maximum of the pass runs on the integer
         // pipes (fpbits.cuh: the IEEE results, bit for bit), leaving the FP64
@@ -261,7 +285,7 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                         o.early = 0;
                         count_solve(ls, hist_s, o);
                         ++L.i;
-                        L.mode = begin_segment(L, net, run, ls, hist_s) ? L_SOLVE : L_DONE;
+                        L.mode = begin_segment(L, net, run, ls, hist_s, slot) ? L_SOLVE : L_DONE;
                     }
                 }
             }

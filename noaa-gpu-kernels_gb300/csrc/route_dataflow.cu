@@ -63,7 +63,7 @@ __device__ __forceinline__ unsigned long long ld_volatile_ull(const unsigned lon
 // complete) and starts its first segment.
 __device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base, const NetDev& net,
                                            const RunDev& run, const DataflowDev& df, LocalStats& ls,
-                                           unsigned int* hist_s)
+                                           unsigned int* hist_s, double2* slot)
 {
     const int R = net.n_reach_int;
 #ifdef TROUTE_CHECK
@@ -100,7 +100,7 @@ __device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base,
     L.q_up_new = 0.0;
     L.q_last = 0.0;
     L.i = 0;
-    L.mode = begin_segment(L, net, run, ls, hist_s) ? L_SOLVE : L_DONE;
+    L.mode = begin_segment(L, net, run, ls, hist_s, slot) ? L_SOLVE : L_DONE;
 }
 
 // Learned starting depth for every lane of the warp whose solve waits for one
@@ -108,7 +108,7 @@ __device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base,
 // bracket [p (1 - delta), p (1 + delta)] around the prediction p. A prediction
 // that is not a positive finite depth below 1e4 m leaves the plain bracket.
 __device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const WarmDev& m, const NetDev& net,
-                                                   const RunDev& run, LocalStats& ls)
+                                                   const RunDev& run, LocalStats& ls, const double2* slot)
 {
     const bool pend = (L.mode == L_SOLVE && L.warm == W_PENDING);
     if (!__any_sync(0xffffffffu, pend)) return;
@@ -119,7 +119,7 @@ __device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const W
         f[1] = warm_feature(pos_to_float(L.quc), true, m.mu[1], m.inv_sd[1]);
         f[2] = warm_feature(pos_to_float(L.qdp), true, m.mu[2], m.inv_sd[2]);
         f[3] = warm_feature(pos_to_float(L.ql), true, m.mu[3], m.inv_sd[3]);
-        const double2 p0 = __ldg(net.prm[0] + L.s), p1 = __ldg(net.prm[1] + L.s), p2 = __ldg(net.prm[2] + L.s);
+        const double2 p0 = slot[0], p1 = slot[kSegSmemStride], p2 = slot[2 * kSegSmemStride];
         f[4] = warm_feature(pos_to_float(p0.x), false, m.mu[4], m.inv_sd[4]);   // dx
         f[5] = warm_feature(pos_to_float(p2.y), false, m.mu[5], m.inv_sd[5]);   // s0
         f[6] = warm_feature(pos_to_float(p1.y), false, m.mu[6], m.inv_sd[6]);   // n
@@ -159,6 +159,8 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
     route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df, WarmDev wm)
 {
     __shared__ unsigned int hist_s[16];
+    __shared__ double2 seg_sm[kParamPlanes * kSegSmemStride];
+    double2* const seg_slot = seg_sm + threadIdx.x;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     WarmSmem& wsm = *reinterpret_cast<WarmSmem*>(dyn_smem);
     if (threadIdx.x < 16) hist_s[threadIdx.x] = 0;
@@ -272,7 +274,7 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
                 failed = true;
             } else if (ri >= 0) {
                 __threadfence();  // the item's inputs were published before it was queued
-                start_item(L, ri, tau, t_base, net, run, df, ls, hist_s);
+                start_item(L, ri, tau, t_base, net, run, df, ls, hist_s, seg_slot);
             } else if (clock64() - L.wait_t0 > run.wait_cycles) {
                 // a slot can legitimately stay empty for long while the run
                 // advances; give up only if no item completed during a whole
@@ -289,10 +291,10 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
         }
 
         // ---- learned starting depths for solves that just began ----
-        if constexpr (WARM) warm_predict_lanes(L, wsm, wm, net, run, ls);
+        if constexpr (WARM) warm_predict_lanes(L, wsm, wm, net, run, ls, seg_slot);
 
         // ---- one depth evaluation per solving lane ----
-        if (__any_sync(kFullMask, L.mode >= L_SOLVE)) lane_pass(L, net, run, ls, hist_s);
+        if (__any_sync(kFullMask, L.mode >= L_SOLVE)) lane_pass(L, net, run, ls, hist_s, seg_slot);
 
         // ---- completed reaches: publish, count dependencies, queue ready items ----
         int npush = 0;
@@ -327,7 +329,7 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
                 const int2 mine = (npush == 2) ? push1 : push0;
                 if (npush == 2) push1 = make_int2(-1, -1);
                 --npush;
-                start_item(L, mine.x, mine.y, t_base, net, run, df, ls, hist_s);
+                start_item(L, mine.x, mine.y, t_base, net, run, df, ls, hist_s, seg_slot);
                 // a reach without solve work completes at once; it is published
                 // in the next pass
             }

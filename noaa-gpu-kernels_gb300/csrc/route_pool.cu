@@ -50,6 +50,8 @@ __device__ __forceinline__ void publish(Lane& L, const NetDev& net)
 __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
 {
     __shared__ unsigned int hist_s[16];
+    __shared__ double2 seg_sm[kParamPlanes * kSegSmemStride];
+    double2* const slot = seg_sm + threadIdx.x;
     __shared__ int2 queue[4][kQCap];
     if (threadIdx.x < 16) hist_s[threadIdx.x] = 0;
     __syncthreads();
@@ -145,7 +147,7 @@ __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
                 L.q_up_new = 0.0;
                 L.q_last = 0.0;
                 L.i = 0;
-                if (begin_segment(L, net, run, ls, hist_s)) {
+                if (begin_segment(L, net, run, ls, hist_s, slot)) {
                     L.mode = L_SOLVE;
                 } else {
                     publish(L, net);
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
             __nanosleep(128);
             continue;
         }
-        lane_pass(L, net, run, ls, hist_s);
+        lane_pass(L, net, run, ls, hist_s, slot);
         if (L.mode == L_DONE) {
             publish(L, net);
             L.mode = L_IDLE;
