@@ -289,8 +289,10 @@ def train_and_plain(T, torch, dev, stream, plain_steps: int, plain_warmup: int, 
     loss = model.fit(pairs.data_ptr(), n, epochs=3, batch=8192, lr=2e-3, seed=1001)
     t_fit = time.perf_counter() - t0
     del pairs
-    # plain single-basin routing, graph-replayed 144-step runs
+    # plain single-basin routing, graph-replayed 144-step runs, in the launch
+    # shape the autotuner picks for it (all mappings; 16-step trials)
     net.set_cfg(T.make_cfg(**TIGHT))
+    tune = net.autotune(ql.data_ptr(), 16, repeats=1, all_mappings=True)
     net.graph_capture(ql.data_ptr(), 144)
     for _ in range(plain_warmup):
         net.graph_launch(stream.cuda_stream)
@@ -310,7 +312,8 @@ def train_and_plain(T, torch, dev, stream, plain_steps: int, plain_warmup: int, 
     plain = {"value": S * 144 * plain_steps / (ms / 1e3), "unit": UNIT,
              "workload": f"{base}: the {S}-segment network alone, plain secant start, 144 steps per graph "
                          f"launch, {plain_steps} timed launches after {plain_warmup}",
-             "iterations_per_solve": st["iterations"] / max(1, st["solves"]), "ms_per_run": ms / plain_steps}
+             "iterations_per_solve": st["iterations"] / max(1, st["solves"]), "ms_per_run": ms / plain_steps,
+             "launch_shape": {k: tune[k] for k in ("mapping", "blocks_per_sm", "threads_per_block", "schedule_flags")}}
     info = {"pairs": int(n), "pair_steps": PAIR_STEPS, "pairs_s": round(t_pairs, 2), "epochs": 3, "batch": 8192,
             "fit_s": round(t_fit, 2), "loss_per_epoch": [round(float(x), 5) for x in loss],
             "delta": WARM_DELTA, "k": WARM_K, "trained_on": f"{base} (seed {w['seed']}), plain run from the initial state"}
