@@ -310,6 +310,11 @@ int troute_debug_timeout_probe(long long wait_cycles);
  * (the last two from CUDA's pow(), for accuracy checks). */
 int troute_debug_pow(const double* x, int n, double* out);
 
+/* Evaluates, on the device, the solver's shared-reciprocal quotient a / b
+ * (one correctly rounded reciprocal, two FMA corrections) for n host pairs,
+ * for comparison with IEEE division. */
+int troute_debug_div(const double* a, const double* b, int n, double* out);
+
 /* ---- schedule and topology helpers ----------------------------------- */
 /* Topological levels as the reference builds them (level 0 = headwater,
  * level = 1 + max upstream level; gen_network.py:219-231). level_ptr needs

@@ -198,6 +198,26 @@ extern "C" int troute_debug_pow(const double* x, int n, double* out)
     return cuda_check(cudaMemcpy(out, dout.p, (size_t)4 * n * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
 }
 
+extern "C" int troute_debug_div(const double* a, const double* b, int n, double* out)
+{
+    if (n < 0 || (n > 0 && (!a || !b || !out))) return set_error(TROUTE_EINVAL, "bad arguments");
+    if (n == 0) return TROUTE_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(TROUTE_ENODEV, "no CUDA device");
+    DevPtr da, db, dout;
+    int rc;
+    const size_t bytes = (size_t)n * sizeof(double);
+    if ((rc = cuda_check(cudaMalloc(&da.p, bytes), "cudaMalloc")) || (rc = cuda_check(cudaMalloc(&db.p, bytes), "cudaMalloc")) ||
+        (rc = cuda_check(cudaMalloc(&dout.p, bytes), "cudaMalloc")) ||
+        (rc = cuda_check(cudaMemcpy(da.p, a, bytes, cudaMemcpyHostToDevice), "H2D")) ||
+        (rc = cuda_check(cudaMemcpy(db.p, b, bytes, cudaMemcpyHostToDevice), "H2D")))
+        return rc;
+    if ((rc = launch_debug_div(static_cast<double*>(da.p), static_cast<double*>(db.p), n, static_cast<double*>(dout.p),
+                               nullptr)))
+        return rc;
+    return cuda_check(cudaMemcpy(out, dout.p, bytes, cudaMemcpyDeviceToHost), "D2H");
+}
+
 // ---------------------------------------------------------------------------
 // topology helpers
 // ---------------------------------------------------------------------------

@@ -103,3 +103,49 @@ __device__ __forceinline__ double twice_chain(double g1, double g2, double g, do
 }
 
 }  // namespace tr
+
+namespace tr {
+
+// Correctly rounded quotients that share one reciprocal.
+//
+// With y = RN(1/b) (CUDA's correctly rounded __drcp_rn), each quotient costs
+// one product and four FMAs instead of a full division: q0 = RN(a y) is within
+// 2 ulp of a/b; one correction q1 = RN(q0 + RN(a - b q0) y) is faithful; then
+// the residual a - b q1 is exact and q2 = RN(q1 + (a - b q1) y) is the
+// correctly rounded a/b (Markstein's theorem, P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990; also Muller et al., Handbook of Floating-Point
+// Arithmetic, the FMA-based division section). The theorem needs normal
+// operands and a normal quotient away from overflow: operands whose exponents
+// are far from that range, zeros, infinities and NaNs take the IEEE division.
+struct SharedRcp {
+    double b, y;
+    bool ok;  // b normal, |b| in [2^-500, 2^501)
+};
+
+__device__ __forceinline__ int dexp(double x) { return (int)(((unsigned long long)dbits(x) >> 52) & 0x7ff); }
+
+__device__ __forceinline__ SharedRcp shared_rcp(double b)
+{
+    SharedRcp r;
+    r.b = b;
+    const int eb = dexp(b);
+    r.ok = eb >= 1023 - 500 && eb <= 1023 + 500;
+    r.y = r.ok ? __drcp_rn(b) : 0.0;
+    return r;
+}
+
+__device__ __forceinline__ double shared_div(double a, const SharedRcp& d)
+{
+    const int ea = dexp(a);
+    // a normal and |a|, |b| in [2^-500, 2^501): |a/b| is far inside the normal
+    // range; else the IEEE division
+    if (!d.ok || ea < 1023 - 500 || ea > 1023 + 500) return a / d.b;
+    double q = a * d.y;
+    double r = __fma_rn(-d.b, q, a);
+    q = __fma_rn(r, d.y, q);
+    r = __fma_rn(-d.b, q, a);
+    return __fma_rn(r, d.y, q);
+}
+
+}  // namespace tr

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "device_common.cuh"
+#include "fpbits.cuh"
 
 namespace tr {
 
@@ -228,6 +229,13 @@ __global__ void velocity_kernel(NetDev net)
     }
 }
 
+__global__ void debug_div_kernel(const double* __restrict__ a, const double* __restrict__ b, int n,
+                                 double* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = shared_div(a[i], shared_rcp(b[i]));
+}
+
 __global__ void debug_pow_kernel(const double* __restrict__ x, int n, double* __restrict__ out)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -312,6 +320,15 @@ int launch_velocity(const NetDev& net, void* stream)
     if (net.n_seg_int <= 0) return TROUTE_OK;
     velocity_kernel<<<grid_for(net.n_seg_int, 256), 256, 0, (cudaStream_t)stream>>>(net);
     return cuda_status(cudaGetLastError(), "velocity launch");
+}
+
+int launch_debug_div(const double* a, const double* b, int n, double* out, void* stream)
+{
+    if (n <= 0) return TROUTE_OK;
+    debug_div_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a, b, n, out);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(TROUTE_ECUDA, "debug_div_kernel: %s", cudaGetErrorString(e));
+    return TROUTE_OK;
 }
 
 int launch_debug_pow(const double* x, int n, double* out, void* stream)

@@ -153,7 +153,9 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
         const double WPC = fp_gt0(above) ? (p.twcc + 2.0 * above) : 0.0;
         const double P = WP + WPC;
         const bool P_pos = fp_gt0(P);
-        const double R = P_pos ? (A + AC) / P : 0.0;
+        // the two quotients by P share one correctly rounded reciprocal
+        const SharedRcp rP = shared_rcp(P_pos ? P : 1.0);
+        const double R = P_pos ? shared_div(A + AC, rP) : 0.0;
         double r23, r53;
         pow23_53(R, &r23, &r53);
         {
@@ -163,7 +165,8 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
             if (fp_gt0(x)) e.Ck = fp_max0(p.ck_fac * ((5.0 / 3.0) * r23 - (2.0 / 3.0) * r53 * (p.sq2 / twl)));
             e.Km = fp_gt0(e.Ck) ? fp_max_pos(dt, p.dx / e.Ck) : dt;
             e.twu = (fp_gt_pos(x, p.bfd) && twcc_pos) ? p.twcc : twl;
-            e.Qmn = P_pos ? (1.0 / ((WP * p.n_ch + WPC * p.ncc) / P)) * (A + AC) * r23 * p.sq_s0 : 0.0;
+            // 1.0 / t is the correctly rounded reciprocal of t
+            e.Qmn = P_pos ? __drcp_rn(shared_div(WP * p.n_ch + WPC * p.ncc, rP)) * (A + AC) * r23 * p.sq_s0 : 0.0;
             if (L.need0) {
                 L.e0 = e;
                 L.need0 = 0;
@@ -179,10 +182,11 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                 }
                 double D0 = e0.Km * (1.0 - X0) + dt / 2.0;
                 if (fp_eq0(D0)) D0 = 1.0;
-                const double c1 = (e0.Km * X0 + dt / 2.0) / D0;
-                const double c2 = (dt / 2.0 - e0.Km * X0) / D0;
-                const double c3 = (e0.Km * (1.0 - X0) - dt / 2.0) / D0;
-                const double c4 = (ql * dt) / D0;
+                const SharedRcp r0 = shared_rcp(D0);
+                const double c1 = shared_div(e0.Km * X0 + dt / 2.0, r0);
+                const double c2 = shared_div(dt / 2.0 - e0.Km * X0, r0);
+                const double c3 = shared_div(e0.Km * (1.0 - X0) - dt / 2.0, r0);
+                const double c4 = shared_div(ql * dt, r0);
                 const double qmc0 = c1 * qup + c2 * quc + c3 * qdp + c4;
                 L.Qj_0 = qmc0 - e0.Qmn;
                 // X at the upper depth, clamped to [0.25, 0.5] (troute_mc_final.cu:105)
@@ -194,10 +198,11 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                 }
                 double D1 = e.Km * (1.0 - X) + dt / 2.0;
                 if (fp_eq0(D1)) D1 = 1.0;
-                const double C1 = (e.Km * X + dt / 2.0) / D1;
-                const double C2 = (dt / 2.0 - e.Km * X) / D1;
-                const double C3 = (e.Km * (1.0 - X) - dt / 2.0) / D1;
-                double C4 = (ql * dt) / D1;
+                const SharedRcp r1 = shared_rcp(D1);
+                const double C1 = shared_div(e.Km * X + dt / 2.0, r1);
+                const double C2 = shared_div(dt / 2.0 - e.Km * X, r1);
+                const double C3 = shared_div(e.Km * (1.0 - X) - dt / 2.0, r1);
+                double C4 = shared_div(ql * dt, r1);
                 const double S3 = C1 * qup + C2 * quc + C3 * qdp;
                 if (fp_lt0(C4) && fp_abs_gt(C4, S3)) C4 = -S3;
                 const double Qj = (S3 + C4) - e.Qmn;

@@ -170,6 +170,7 @@ _SIGS = {
     "troute_write_network": ([C.c_char_p, _P], _I),
     "troute_debug_timeout_probe": ([C.c_longlong], _I),
     "troute_debug_pow": ([_P, _I, _P], _I),
+    "troute_debug_div": ([_P, _P, _I, _P], _I),
     "troute_levels": ([_I, _P, _P, _P, _P, _P, _P], _I),
     "troute_validate": ([_P], _I),
     "troute_gen_tree": ([_U64, _I, _I, _I, _P, _P, _P, _P], _I),
@@ -256,6 +257,15 @@ def debug_pow(x):
     out = np.zeros(4 * x.size)
     _check(lib().troute_debug_pow(_ptr(x), int(x.size), _ptr(out)))
     return tuple(out.reshape(4, -1))
+
+
+def debug_div(a, b):
+    """The solver's shared-reciprocal quotient a / b evaluated on the device."""
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    out = np.zeros_like(a)
+    _check(lib().troute_debug_div(_ptr(a), _ptr(b), a.size, _ptr(out)))
+    return out
 
 
 def device_info() -> dict:

@@ -364,3 +364,32 @@ def test_autotuner_keeps_state_and_results():
         qb = b.get_state()
     for x, y in zip(qa, qb):
         np.testing.assert_array_equal(x, y)
+
+
+def test_shared_reciprocal_division_is_ieee():
+    """The solver's quotients that share one reciprocal (Markstein's
+    correction) equal IEEE division bit for bit: random operands over the
+    whole exponent range (the far ranges take the IEEE path), significands of
+    all ones and powers of two, the solver's own operand ranges, zeros,
+    infinities and NaNs."""
+    rng = np.random.default_rng(23)
+    n = 2_000_000
+    a = np.ldexp(rng.uniform(1, 2, n), rng.integers(-1070, 1024, n)) * rng.choice([-1, 1], n)
+    b = np.ldexp(rng.uniform(1, 2, n), rng.integers(-1070, 1024, n)) * rng.choice([-1, 1], n)
+    # the coefficient divisions of the solver: numerators up to ~1e6, denominators 150..1e9
+    a2 = rng.uniform(-1e6, 1e6, n)
+    b2 = np.exp(rng.uniform(np.log(150.0), np.log(1e9), n))
+    allones = np.ldexp(2.0 - np.ldexp(1.0, -52), rng.integers(-60, 60, 200000))
+    pow2 = np.ldexp(1.0, rng.integers(-60, 60, 200000))
+    a3 = np.concatenate([allones, pow2, rng.uniform(1, 2, 200000), allones])
+    b3 = np.concatenate([rng.uniform(1, 2, 200000), allones, allones, pow2])
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, 5e-324, 1e308])
+    a4 = np.repeat(special, special.size)
+    b4 = np.tile(special, special.size)
+    A = np.concatenate([a, a2, a3, a4])
+    B = np.concatenate([b, b2, b3, b4])
+    with np.errstate(all="ignore"):
+        ref = A / B
+    got = T.debug_div(A, B)
+    same = (got.view(np.int64) == ref.view(np.int64)) | (np.isnan(got) & np.isnan(ref))
+    assert same.all(), (A[~same][:5], B[~same][:5], got[~same][:5], ref[~same][:5])
