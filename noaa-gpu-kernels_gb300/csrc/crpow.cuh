@@ -23,7 +23,9 @@
 //      round(y z + (err(y z) + y delta + y z e' ln x)), each scaled back by
 //      2^(2k), 2^(5k) (exact).
 // The rounding of step 4 is therefore the correctly rounded result except when
-// the exact value lies within ~2^-84 relative of a rounding midpoint. The
+// the exact value lies within ~2^-72 relative of a rounding midpoint (the
+// ~1e-16 exponent-offset term is formed from the seed's single-precision
+// log2, and on the device in single precision: ~2^-24 of it). The
 // host C library's pow() is correctly rounded in all but rare cases, so the
 // device solver reproduces the host computation bit for bit almost always.
 // Only IEEE operations and explicit fma() are used, so compiling without
@@ -64,19 +66,38 @@ CRPOW_HD double crpow_from_bits(uint64_t b)
 #endif
 }
 
+#if defined(__CUDA_ARCH__)
+// Float <-> double conversions for the seed, on the integer pipe (the FP64
+// pipe is the solver's bottleneck): y in [1, 8) truncated to float; a normal
+// float (or +0) widened exactly.
+__device__ __forceinline__ float crpow_y_to_float(double y)
+{
+    const long long b = __double_as_longlong(y);
+    return __int_as_float((int)(((b >> 52) - 896) << 23) | (int)((b >> 29) & 0x7fffff));
+}
+__device__ __forceinline__ double crpow_widen(float f)
+{
+    const unsigned fb = __float_as_uint(f);
+    if ((fb << 1) == 0) return 0.0;
+    const unsigned long long sign = (unsigned long long)(fb >> 31) << 63;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(((fb >> 23) & 0xff) + 896) << 52) |
+                                            ((unsigned long long)(fb & 0x7fffff) << 29)));
+}
+#endif
+
 // Single-precision log2(y) and seed of y^(-1/3) for y in [1, 8).
-CRPOW_HD void crpow_seed(double y, double* log2y, double* rinv)
+CRPOW_HD void crpow_seed(double y, float* log2y, double* rinv)
 {
 #if defined(__CUDA_ARCH__)
-    const float yf = (float)y;
+    const float yf = crpow_y_to_float(y);
     float l, r;
     asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l) : "f"(yf));
     const float e = l * (-1.0f / 3.0f);
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(e));
-    *log2y = (double)l;
-    *rinv = (double)r;
+    *log2y = l;
+    *rinv = crpow_widen(r);
 #else
-    *log2y = (double)std::log2((float)y);
+    *log2y = std::log2((float)y);
     *rinv = (double)(1.0f / std::cbrt((float)y));
 #endif
 }
@@ -87,6 +108,15 @@ CRPOW_HD double crpow_exp2i(int n) { return crpow_from_bits((uint64_t)(1023 + n)
 // Scales v by 2^n (n may exceed the single-step range); exact for normal results.
 CRPOW_HD double crpow_scale(double v, int n)
 {
+#if defined(__CUDA_ARCH__)
+    {
+        // a normal result: add n to the exponent field on the integer pipe
+        const long long b = __double_as_longlong(v);
+        const int ev = (int)((b >> 52) & 0x7ff);
+        if (ev != 0 && ev != 0x7ff && ev + n >= 1 && ev + n <= 0x7fe)
+            return __longlong_as_double(b + ((long long)n << 52));
+    }
+#endif
     while (n > 1000) { v *= crpow_exp2i(1000); n -= 1000; }
     while (n < -1000) { v *= crpow_exp2i(-1000); n += 1000; }
     return v * crpow_exp2i(n);
@@ -100,7 +130,13 @@ constexpr double kFl53Minus53 = 7.401486830834377e-17;
 // x = 0 gives 0, +inf gives +inf, NaN propagates, like pow().
 CRPOW_HD void pow23_53(double x, double* p23, double* p53)
 {
-    if (!(x > 0.0)) {
+#if defined(__CUDA_ARCH__)
+    const long long xb = __double_as_longlong(x);
+    const bool x_pos = xb > 0 && xb <= 0x7ff0000000000000ll;  // x > 0 (integer pipe)
+#else
+    const bool x_pos = x > 0.0;
+#endif
+    if (!x_pos) {
         const double v = (x == 0.0) ? 0.0 : (x - x) / (x - x);  // 0 or NaN
         *p23 = v;
         *p53 = v;
@@ -126,7 +162,8 @@ CRPOW_HD void pow23_53(double x, double* p23, double* p53)
     const double y = crpow_from_bits((b & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(1023 + j) << 52));
 
     const double third = 1.0 / 3.0;
-    double r, log2y;
+    double r;
+    float log2y;
     crpow_seed(y, &log2y, &r);
     {
         const double r3 = (r * r) * r;
@@ -147,8 +184,23 @@ CRPOW_HD void pow23_53(double x, double* p23, double* p53)
     const double delta = -(d * (r2 * r2)) * third;
     // exponent offset: x^fl(2/3) = x^(2/3) (1 + (fl(2/3) - 2/3) ln x), same for 5/3;
     // ln x needs only ~1e-3 relative accuracy here (the term is ~1e-16 x^(2/3))
-    const double lnx = (log2y + 3.0 * (double)k) * 0.6931471805599453;
+#if defined(__CUDA_ARCH__)
+    double c2, c5;
+    if (k >= -8 && k <= 8) {
+        // |ln x| < 19: the correction terms (< 1.5e-15) in single precision on
+        // the FP32 pipe, off by less than 2^-72 of the result
+        const float lnxf = (log2y + 3.0f * (float)k) * 0.6931472f;
+        c2 = crpow_widen((float)kFl23Minus23 * lnxf);
+        c5 = crpow_widen((float)kFl53Minus53 * lnxf);
+    } else {
+        const double lnx = (crpow_widen(log2y) + 3.0 * (double)k) * 0.6931471805599453;
+        c2 = kFl23Minus23 * lnx;
+        c5 = kFl53Minus53 * lnx;
+    }
+#else
+    const double lnx = ((double)log2y + 3.0 * (double)k) * 0.6931471805599453;
     const double c2 = kFl23Minus23 * lnx, c5 = kFl53Minus53 * lnx;
+#endif
     const double z23 = z + (delta + z * c2);
     const double w0 = y * z;
     const double we = fma(y, z, -w0);
