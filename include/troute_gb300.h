@@ -315,6 +315,12 @@ int troute_debug_pow(const double* x, int n, double* out);
  * for comparison with IEEE division. */
 int troute_debug_div(const double* a, const double* b, int n, double* out);
 
+/* Evaluates, on the device, the solver's convergence comparison
+ * (a / b > c, IEEE quotient, b > 0, c > 0) the way the secant pass does it
+ * (an FMA residual against the rounding midpoint above c, IEEE division only
+ * in ambiguous cases): out[i] = 1 or 0, for comparison with the host. */
+int troute_debug_quot_gt(const double* a, const double* b, double c, int n, int* out);
+
 /* ---- schedule and topology helpers ----------------------------------- */
 /* Topological levels as the reference builds them (level 0 = headwater,
  * level = 1 + max upstream level; gen_network.py:219-231). level_ptr needs

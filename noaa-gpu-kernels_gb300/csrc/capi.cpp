@@ -198,7 +198,10 @@ extern "C" int troute_debug_pow(const double* x, int n, double* out)
     return cuda_check(cudaMemcpy(out, dout.p, (size_t)4 * n * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
 }
 
-extern "C" int troute_debug_div(const double* a, const double* b, int n, double* out)
+// Device evaluation of a binary operation of the solver on n host pairs:
+// `cols` result columns of n doubles each (launch writes them).
+template <class L>
+static int debug_binary(const double* a, const double* b, int n, double* out, int cols, L launch)
 {
     if (n < 0 || (n > 0 && (!a || !b || !out))) return set_error(TROUTE_EINVAL, "bad arguments");
     if (n == 0) return TROUTE_OK;
@@ -208,14 +211,41 @@ extern "C" int troute_debug_div(const double* a, const double* b, int n, double*
     int rc;
     const size_t bytes = (size_t)n * sizeof(double);
     if ((rc = cuda_check(cudaMalloc(&da.p, bytes), "cudaMalloc")) || (rc = cuda_check(cudaMalloc(&db.p, bytes), "cudaMalloc")) ||
-        (rc = cuda_check(cudaMalloc(&dout.p, bytes), "cudaMalloc")) ||
+        (rc = cuda_check(cudaMalloc(&dout.p, cols * bytes), "cudaMalloc")) ||
         (rc = cuda_check(cudaMemcpy(da.p, a, bytes, cudaMemcpyHostToDevice), "H2D")) ||
         (rc = cuda_check(cudaMemcpy(db.p, b, bytes, cudaMemcpyHostToDevice), "H2D")))
         return rc;
-    if ((rc = launch_debug_div(static_cast<double*>(da.p), static_cast<double*>(db.p), n, static_cast<double*>(dout.p),
-                               nullptr)))
+    if ((rc = launch(static_cast<double*>(da.p), static_cast<double*>(db.p), n, static_cast<double*>(dout.p))))
         return rc;
-    return cuda_check(cudaMemcpy(out, dout.p, bytes, cudaMemcpyDeviceToHost), "D2H");
+    return cuda_check(cudaMemcpy(out, dout.p, cols * bytes, cudaMemcpyDeviceToHost), "D2H");
+}
+
+extern "C" int troute_debug_div(const double* a, const double* b, int n, double* out)
+{
+    return debug_binary(a, b, n, out, 1, [](const double* da, const double* db, int m, double* o) {
+        return launch_debug_div(da, db, m, o, nullptr);
+    });
+}
+
+extern "C" int troute_debug_quot_gt(const double* a, const double* b, double c, int n, int* out)
+{
+    if (n < 0 || (n > 0 && (!a || !b || !out))) return set_error(TROUTE_EINVAL, "bad arguments");
+    if (!(c > 0.0)) return set_error(TROUTE_EINVAL, "c must be > 0");
+    if (n == 0) return TROUTE_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(TROUTE_ENODEV, "no CUDA device");
+    DevPtr da, db, dout;
+    int rc;
+    const size_t bytes = (size_t)n * sizeof(double);
+    if ((rc = cuda_check(cudaMalloc(&da.p, bytes), "cudaMalloc")) || (rc = cuda_check(cudaMalloc(&db.p, bytes), "cudaMalloc")) ||
+        (rc = cuda_check(cudaMalloc(&dout.p, (size_t)n * sizeof(int)), "cudaMalloc")) ||
+        (rc = cuda_check(cudaMemcpy(da.p, a, bytes, cudaMemcpyHostToDevice), "H2D")) ||
+        (rc = cuda_check(cudaMemcpy(db.p, b, bytes, cudaMemcpyHostToDevice), "H2D")))
+        return rc;
+    if ((rc = launch_debug_quot_gt(static_cast<double*>(da.p), static_cast<double*>(db.p), c, n,
+                                   static_cast<int*>(dout.p), nullptr)))
+        return rc;
+    return cuda_check(cudaMemcpy(out, dout.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost), "D2H");
 }
 
 // ---------------------------------------------------------------------------

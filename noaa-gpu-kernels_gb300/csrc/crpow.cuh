@@ -23,11 +23,12 @@
 //      round(y z + (err(y z) + y delta + y z e' ln x)), each scaled back by
 //      2^(2k), 2^(5k) (exact).
 // The rounding of step 4 is therefore the correctly rounded result except when
-// the exact value lies within ~2^-72 relative of a rounding midpoint (the
+// the exact value lies within ~2^-74 relative of a rounding midpoint (the
 // ~1e-16 exponent-offset term is formed from the seed's single-precision
-// log2, and on the device in single precision: ~2^-24 of it). The
-// host C library's pow() is correctly rounded in all but rare cases, so the
-// device solver reproduces the host computation bit for bit almost always.
+// log2, and on the device for x in [2^-9, 2^9) in single precision: ~2^-24
+// of it). Host and device forms agree on all but ~1e-7 of arguments. The C
+// library's pow() (glibc) is not correctly rounded: it differs from these
+// results by one ulp on ~0.2 % of arguments.
 // Only IEEE operations and explicit fma() are used, so compiling without
 // implicit FMA contraction does not change these results.
 #pragma once
@@ -186,9 +187,9 @@ CRPOW_HD void pow23_53(double x, double* p23, double* p53)
     // ln x needs only ~1e-3 relative accuracy here (the term is ~1e-16 x^(2/3))
 #if defined(__CUDA_ARCH__)
     double c2, c5;
-    if (k >= -8 && k <= 8) {
-        // |ln x| < 19: the correction terms (< 1.5e-15) in single precision on
-        // the FP32 pipe, off by less than 2^-72 of the result
+    if (k >= -3 && k <= 2) {
+        // x in [2^-9, 2^9), |ln x| < 6.3: the correction terms (< 5e-16) in
+        // single precision on the FP32 pipe, off by less than 2^-74 of the result
         const float lnxf = (log2y + 3.0f * (float)k) * 0.6931472f;
         c2 = crpow_widen((float)kFl23Minus23 * lnxf);
         c5 = crpow_widen((float)kFl53Minus53 * lnxf);

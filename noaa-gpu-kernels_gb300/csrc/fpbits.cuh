@@ -148,4 +148,29 @@ __device__ __forceinline__ double shared_div(double a, const SharedRcp& d)
     return __fma_rn(r, d.y, q);
 }
 
+// RN(a / b) > c -- the IEEE quotient compared with c -- for any a, b > 0 and
+// c > 0 (neither NaN), mostly without the division. RN(a/b) > c exactly when
+// a/b lies above the midpoint m = c + u between c and the next double
+// (u = ulp(c)/2, a power of two), up to the tie a/b = m. With x = a - c b and
+// y = u b (exact for b and c normal, y normal): a/b > m <=> x > y. The FMA
+// gives e = RN(x) with one rounding, and rounding is monotone with y
+// representable, so e > y implies x > y and e < y implies x < y. Only e == y
+// (a tie, or x within half an ulp of y), NaN and operands outside the normal
+// range take the division.
+__device__ __forceinline__ bool quot_gt_pos(double a, double b, double c)
+{
+    const int eb = dexp(b), ec = dexp(c);
+    const int k = ec - 1023 - 53;  // u = 2^k
+    if ((unsigned)(eb - 1) < 0x7feu && (unsigned)(ec - 1) < 0x7feu && (unsigned)(eb + k - 1) < 0x7feu) {
+        const double y = __longlong_as_double(dbits(b) + ((long long)k << 52));
+        const double e = __fma_rn(-c, b, a);
+        if (fp_gt_pos(e, y)) return true;
+        if (fp_lt_pos(e, y)) return false;
+    }
+    return fp_gt_pos(a / b, c);
+}
+
+// |x| on the integer pipe
+__device__ __forceinline__ double fp_abs(double x) { return __longlong_as_double(dbits(x) & 0x7fffffffffffffffll); }
+
 }  // namespace tr

@@ -236,6 +236,13 @@ __global__ void debug_div_kernel(const double* __restrict__ a, const double* __r
     if (i < n) out[i] = shared_div(a[i], shared_rcp(b[i]));
 }
 
+__global__ void debug_quot_gt_kernel(const double* __restrict__ a, const double* __restrict__ b, double c, int n,
+                                     int* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = quot_gt_pos(a[i], b[i], c) ? 1 : 0;
+}
+
 __global__ void debug_pow_kernel(const double* __restrict__ x, int n, double* __restrict__ out)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -329,6 +336,13 @@ int launch_debug_div(const double* a, const double* b, int n, double* out, void*
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(TROUTE_ECUDA, "debug_div_kernel: %s", cudaGetErrorString(e));
     return TROUTE_OK;
+}
+
+int launch_debug_quot_gt(const double* a, const double* b, double c, int n, int* out, void* stream)
+{
+    if (n <= 0) return TROUTE_OK;
+    debug_quot_gt_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a, b, c, n, out);
+    return cuda_status(cudaGetLastError(), "debug quotient comparison launch");
 }
 
 int launch_debug_pow(const double* x, int n, double* out, void* stream)

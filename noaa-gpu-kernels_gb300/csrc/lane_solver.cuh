@@ -220,20 +220,22 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                 const double dQ = L.Qj_0 - Qj;
                 double h_1 = !fp_eq0(dQ) ? h - (Qj * (L.h_0 - h)) / dQ : h;
                 if (fp_lt0(h_1)) h_1 = h;
-                double rerr, aerr;
+                // the reference's test rerr > rtol && aerr >= atol with
+                // rerr = |(h_1 - h) / h|, aerr = |h_1 - h| (rerr = 0, aerr = 0.9
+                // for h <= 0); the relative error's quotient is only compared
+                // with rtol, which quot_gt_pos does exactly without dividing
+                bool more;
                 if (fp_gt0(h)) {
-                    rerr = fabs((h_1 - h) / h);
-                    aerr = fabs(h_1 - h);
+                    const double aerr = fp_abs(h_1 - h);
+                    more = fp_ge_nonneg(aerr, tol.atol) && quot_gt_pos(aerr, h, tol.rtol);
                 } else {
-                    rerr = 0.0;
-                    aerr = 0.9;
+                    more = fp_gt_pos(0.0, tol.rtol) && fp_ge_nonneg(0.9, tol.atol);
                 }
                 L.h_0 = fp_max0(h);
                 L.h = fp_max0(h_1);
                 L.e0 = e;
                 ++L.iter;
                 ++L.total;
-                const bool more = fp_gt_pos(rerr, tol.rtol) && fp_ge_nonneg(aerr, tol.atol);
                 bool stop;
                 if (L.warm == W_ACTIVE) {
                     // warm phase: accepted once the stop test passes at a depth of at

@@ -166,6 +166,7 @@ int launch_gather(const double* src, const long long* map, long long n, double* 
 int launch_timeout_probe(DevStats* stats, long long wait_cycles, void* stream);
 int launch_debug_pow(const double* x, int n, double* out, void* stream);
 int launch_debug_div(const double* a, const double* b, int n, double* out, void* stream);
+int launch_debug_quot_gt(const double* a, const double* b, double c, int n, int* out, void* stream);
 int launch_velocity(const NetDev& net, void* stream);
 
 }  // namespace tr

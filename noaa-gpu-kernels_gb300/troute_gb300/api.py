@@ -171,6 +171,7 @@ _SIGS = {
     "troute_debug_timeout_probe": ([C.c_longlong], _I),
     "troute_debug_pow": ([_P, _I, _P], _I),
     "troute_debug_div": ([_P, _P, _I, _P], _I),
+    "troute_debug_quot_gt": ([_P, _P, C.c_double, _I, _P], _I),
     "troute_levels": ([_I, _P, _P, _P, _P, _P, _P], _I),
     "troute_validate": ([_P], _I),
     "troute_gen_tree": ([_U64, _I, _I, _I, _P, _P, _P, _P], _I),
@@ -266,6 +267,16 @@ def debug_div(a, b):
     out = np.zeros_like(a)
     _check(lib().troute_debug_div(_ptr(a), _ptr(b), a.size, _ptr(out)))
     return out
+
+
+def debug_quot_gt(a, b, c):
+    """The solver's convergence comparison a / b > c evaluated on the device
+    (boolean array)."""
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    out = np.zeros(a.size, np.int32)
+    _check(lib().troute_debug_quot_gt(_ptr(a), _ptr(b), float(c), a.size, _ptr(out)))
+    return out.astype(bool)
 
 
 def device_info() -> dict:

@@ -236,14 +236,16 @@ def test_checkpoint_resume_is_bit_identical():
 
 def test_launch_shape_does_not_change_results():
     """The schedule (grid size, block shape, reach-to-warp mapping, which lane
-    takes which reach) is not part of the arithmetic: identical bits for all."""
+    takes which reach, whether a lane continues with an item it made ready)
+    is not part of the arithmetic: identical bits for all."""
     c = synth.network("tree:20000", seed=8, n_ts=16)
     args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
     ref = None
-    for mapping, shapes in ((3, ((0, 0), (128, 1), (128, 2))), (2, ((0, 0), (128, 1))),
-                            (1, ((128, 0), (64, 1), (32, 2)))):
-        outs = [T.route_tree(*args, cfg=T.make_cfg(mapping=mapping, threads_per_block=tpb, blocks_per_sm=bps))["q"]
-                for tpb, bps in shapes]
+    for mapping, shapes in ((3, ((0, 0, 0), (128, 1, 0), (128, 2, 1), (0, 0, 1))),
+                            (2, ((0, 0, 0), (128, 1, 0))), (1, ((128, 0, 0), (64, 1, 0), (32, 2, 0)))):
+        outs = [T.route_tree(*args, cfg=T.make_cfg(mapping=mapping, threads_per_block=tpb, blocks_per_sm=bps,
+                                                   schedule_flags=fl))["q"]
+                for tpb, bps, fl in shapes]
         if ref is None:
             ref = outs[0]
         for x in outs:
@@ -364,6 +366,38 @@ def test_autotuner_keeps_state_and_results():
         qb = b.get_state()
     for x, y in zip(qa, qb):
         np.testing.assert_array_equal(x, y)
+
+
+def test_convergence_comparison_matches_ieee_quotient():
+    """The secant pass's stop test compares |h_1 - h| / h with rtol through an
+    FMA residual instead of dividing; it must give the IEEE quotient's answer
+    for every operand: quotients within a few ulps of rtol and of the rounding
+    midpoint above it, random operands over the whole range, subnormal,
+    infinite, zero and NaN operands, several rtol values."""
+    rng = np.random.default_rng(31)
+    for c in (1e-8, 0.01, 1e-6, 0.3, 2.0 ** -30, np.nextafter(1e-8, 1.0)):
+        n = 400_000
+        b = np.exp(rng.uniform(np.log(1e-4), np.log(1e4), n))
+        a0 = b * c
+        steps = rng.integers(-6, 7, n)
+        a = a0.copy()
+        for j in range(1, 7):
+            a = np.where(steps >= j, np.nextafter(a, np.inf), a)
+            a = np.where(steps <= -j, np.nextafter(a, -np.inf), a)
+        # random magnitudes over the whole range
+        a2 = np.ldexp(rng.uniform(1, 2, n), rng.integers(-1074, 1024, n))
+        b2 = np.ldexp(rng.uniform(1, 2, n), rng.integers(-1074, 1024, n))
+        special = np.array([0.0, np.inf, np.nan, 5e-324, 1e-310, 1e308, 1.0, c])
+        a3 = np.repeat(special, 4)
+        b3 = np.tile(np.array([5e-324, 1e-310, 1.0, 1e308]), special.size)
+        A = np.concatenate([a, a2, a3])
+        B = np.concatenate([b, b2, b3])
+        with np.errstate(all="ignore"):
+            ref = (A / B) > c
+        got = T.debug_quot_gt(A, B, c)
+        bad = got != ref
+        assert not bad.any(), (c, A[bad][:5], B[bad][:5])
+        assert 0.2 < ref[:n].mean() < 0.8  # the first set straddles c
 
 
 def test_shared_reciprocal_division_is_ieee():

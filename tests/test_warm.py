@@ -208,10 +208,10 @@ def c0_model():
     return m
 
 
-@pytest.mark.parametrize("delta,k", [(0.05, 16), (0.01, 4)])
-def test_warm_routing_replays_bit_identically_in_the_oracle(c0_model, delta, k):
+@pytest.mark.parametrize("delta,k,flags", [(0.05, 16, 0), (0.01, 4, 0), (0.05, 16, 1)])
+def test_warm_routing_replays_bit_identically_in_the_oracle(c0_model, delta, k, flags):
     c = synth.network("c0", seed=77, n_ts=30)
-    cfg = tight_cfg(warm_start=1, warm_k=k, record_history=1, record_start=1)
+    cfg = tight_cfg(warm_start=1, warm_k=k, record_history=1, record_start=1, schedule_flags=flags)
     with T.Network(c["topo"], c["params"], cfg=cfg) as net:
         net.set_warm_start(c0_model, delta)
         net.set_state(c["q0"], c["d0"], c["rl0"])
