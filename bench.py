@@ -529,7 +529,9 @@ def run_ours(args, dist: Dist):
             "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
                        "early_exits": stats["early_exits"], "warm_used": stats["warm_used"],
                        "warm_fallback_rate": stats["warm_fallback"] / max(1, stats["warm_used"]),
-                       "busy_lanes_per_warp_pass": stats["lane_busy"] / max(1, stats["warp_passes"])}}
+                       "busy_lanes_per_warp_pass": stats["lane_busy"] / max(1, stats["warp_passes"]),
+                       "busy_lanes_per_solving_pass": stats["lane_busy"] / max(1, stats["solve_passes"]),
+                       "solving_passes_share": stats["solve_passes"] / max(1, stats["warp_passes"])}}
     if tune:
         line["autotune"] = tune
     if model:

@@ -84,6 +84,8 @@ typedef struct troute_stats {
     unsigned long long lane_busy;     /* lane-passes spent evaluating a depth */
     unsigned long long lane_wait;     /* lane-passes waiting for inputs */
     unsigned long long lane_idle;     /* lane-passes with no work */
+    unsigned long long solve_passes;  /* warp passes that evaluated at least one depth
+                                         (lane_busy / solve_passes: lanes per FP64 instruction) */
     double kernel_ms;                 /* device time of the routing kernel(s) */
     int timeout;                      /* 1 if a bounded wait ran out */
     int reserved[3];

@@ -994,6 +994,7 @@ static int collect(troute_handle* H, troute_stats* stats, bool timed)
         stats->lane_busy = ds.lane_busy;
         stats->lane_wait = ds.lane_wait;
         stats->lane_idle = ds.lane_idle;
+        stats->solve_passes = ds.solve_passes;
         stats->timeout = ds.error == TROUTE_ETIMEOUT;
         if (timed) {
             float ms = 0.f;

@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
     long long queued_since = -1;  // lane 0: when this idle warp first saw unclaimed items
     Lane L;
     L.mode = L_IDLE;
-    unsigned long long n_pass = 0, n_busy = 0, n_wait = 0, n_idle = 0;
+    unsigned long long n_pass = 0, n_busy = 0, n_wait = 0, n_idle = 0, n_solve = 0;
     unsigned idle_ns = kSleepMinNs;  // warp-uniform
     unsigned long long idle_seen = ~0ull;  // warp-uniform: n_done when this warp last saw progress
     long long idle_t0 = clock64();
@@ -294,7 +294,10 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
         if constexpr (WARM) warm_predict_lanes(L, wsm, wm, net, run, ls, seg_slot);
 
         // ---- one depth evaluation per solving lane ----
-        if (__any_sync(kFullMask, L.mode >= L_SOLVE)) lane_pass(L, net, run, ls, hist_s, seg_slot);
+        if (__any_sync(kFullMask, L.mode >= L_SOLVE)) {
+            n_solve++;
+            lane_pass(L, net, run, ls, hist_s, seg_slot);
+        }
 
         // ---- completed reaches: publish, count dependencies, queue ready items ----
         int npush = 0;
@@ -384,6 +387,7 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
         atomicAdd(&run.stats->lane_busy, n_busy);
         atomicAdd(&run.stats->lane_wait, n_wait);
         atomicAdd(&run.stats->lane_idle, n_idle);
+        atomicAdd(&run.stats->solve_passes, n_solve);
     }
     flush_stats(ls, hist_s, run.stats);
 }

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
     bool failed = false;
     Lane L;
     L.mode = L_IDLE;
-    unsigned long long n_pass = 0, n_busy = 0, n_wait = 0, n_idle = 0;  // lane 0's tallies
+    unsigned long long n_pass = 0, n_busy = 0, n_wait = 0, n_idle = 0, n_solve = 0;  // lane 0's tallies
 
     while (true) {
         // ---- refill the warp queue with one level-block when lanes are idle ----
@@ -166,6 +166,7 @@ __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
             __nanosleep(128);
             continue;
         }
+        n_solve++;
         lane_pass(L, net, run, ls, hist_s, slot);
         if (L.mode == L_DONE) {
             publish(L, net);
@@ -178,6 +179,7 @@ __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
         atomicAdd(&run.stats->lane_busy, n_busy);
         atomicAdd(&run.stats->lane_wait, n_wait);
         atomicAdd(&run.stats->lane_idle, n_idle);
+        atomicAdd(&run.stats->solve_passes, n_solve);
     }
     flush_stats(ls, hist_s, run.stats);
 }

@@ -70,7 +70,7 @@ TR_HD inline SegP derive_seg(const troute_chparams& c)
 struct DevStats {
     unsigned long long solves, iterations, retries, early_exits, warm_used, warm_fallback;
     unsigned long long hist[16];
-    unsigned long long warp_passes, lane_busy, lane_wait, lane_idle;
+    unsigned long long warp_passes, lane_busy, lane_wait, lane_idle, solve_passes;
     int error;       // 0 ok, TROUTE_ETIMEOUT, TROUTE_EINVAL (bad index seen)
     int err_reach;   // internal reach of the first failure
     int err_step;    // step of the first failure

@@ -79,6 +79,7 @@ class Stats(C.Structure):
         ("lane_busy", C.c_ulonglong),
         ("lane_wait", C.c_ulonglong),
         ("lane_idle", C.c_ulonglong),
+        ("solve_passes", C.c_ulonglong),
         ("kernel_ms", C.c_double),
         ("timeout", C.c_int),
         ("reserved", C.c_int * 3),
@@ -97,6 +98,7 @@ class Stats(C.Structure):
             "lane_busy": int(self.lane_busy),
             "lane_wait": int(self.lane_wait),
             "lane_idle": int(self.lane_idle),
+            "solve_passes": int(self.solve_passes),
             "kernel_ms": float(self.kernel_ms),
             "timeout": int(self.timeout),
         }
