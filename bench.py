@@ -177,7 +177,7 @@ def measured_peak_hbm():
 def profiled(key: str, warm: bool):
     """A figure of the routing kernel from the committed ncu summary: the
     warm-started kernel's (an ensemble capture) or the plain kernel's."""
-    name = "route_dataflow_warm_ens64.md" if warm else "route_kernel_c1.md"
+    name = "route_dataflow_warm_ens256.md" if warm else "route_kernel_c1.md"
     p = os.path.join(ROOT, "profiles", name)
     try:
         for ln in open(p):
