@@ -1,0 +1,195 @@
+"""Every benchmark configuration at full network size on the GPU against the
+FP64 CPU oracle (the reference's algorithm restated; run here with all host
+threads, level-parallel, which does not change its results), with the
+maximum relative error on discharge reported for every config:
+
+- at the reference's tolerance (rtol 0.01), against the oracle with the C
+  library's pow() -- the reference's own arithmetic, bit-identical to its
+  compiled routine: max relative error below 1e-10;
+- at rtol 1e-8, against the oracle with correctly rounded powers (the
+  arithmetic the GPU uses): bit-identical (max relative error 0), also for
+  the learned warm start replayed from the starting depths the GPU used;
+- at rtol 1e-8 against the C-library-pow oracle the error is printed only:
+  at that tolerance the reference's secant is ulp-sensitive (its limit
+  depends on the starting bracket), so one misrounded power can move a
+  converged depth by far more than an ulp.
+
+Configs: c1 (2.7 M segments, 2 steps), c2 (256 basins, 12.0 M segments,
+1 step), c4 (64 members of c1, 1 step, members 0 and 63 checked), c4w (c4
+with the learned warm start), c3 (a fresh-seed c1 network routed with the
+model trained on c1), from the initial state. Each line printed is
+`PARITY <config> <tolerance> <oracle> max_rel=<value>`.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import troute_gb300 as T
+from oracle import troute_oracle as O
+from troute_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+REF = O.REF_TOL
+TIGHT = (1e-8, 1e-10, 100, 5)
+THREADS = max(1, os.cpu_count() or 1)
+MEMBERS = (0, 63)
+
+
+def cfg_of(tol, **kw):
+    return T.make_cfg(rtol=tol[0], atol=tol[1], maxiter=tol[2], attempts=tol[3], **kw)
+
+
+def max_rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    same = a == b
+    den = np.maximum(np.abs(b), 1e-300)
+    return float(np.max(np.where(same, 0.0, np.abs(a - b) / den))) if a.size else 0.0
+
+
+def report(config, tol, oracle, err):
+    print(f"\nPARITY {config} rtol={tol[0]:g} {oracle} max_rel={err:.3e}")
+
+
+def oracle(net, params, qlat, tol, mode, **kw):
+    with O.pow_mode(mode):
+        return O.route_tree(net["topo"], params, qlat, net["q0"], net["d0"], net["rl0"], tol=tol,
+                            threads=THREADS, **kw)
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return synth.network("c1", n_ts=2)
+
+
+@pytest.fixture(scope="module")
+def members(c1):
+    S = c1["topo"]["n_segments"]
+    qf, nf = np.empty((64, S)), np.empty((64, S))
+    for m in range(64):
+        qf[m], nf[m] = synth.make_member(1004, m, S)
+    return qf, nf
+
+
+@pytest.fixture(scope="module")
+def model():
+    """The bench's recipe: pairs of an 18-step plain c1 run, 3 epochs."""
+    torch = pytest.importorskip("torch")
+    w = synth.network("c1", n_ts=18)
+    dev = torch.device("cuda", 0)
+    ql = torch.from_numpy(np.ascontiguousarray(w["qlat"])).to(dev)
+    with T.Network(w["topo"], w["params"], cfg=cfg_of(TIGHT, record_pairs=1)) as net:
+        net.set_state(w["q0"], w["d0"], w["rl0"])
+        net.run_device(ql.data_ptr(), 18)
+        net.sync()
+        n = net.pairs()
+        pairs = torch.empty((n, 9), dtype=torch.float32, device=dev)
+        net.pairs(pairs.data_ptr(), n)
+    m = T.WarmModel(1001)
+    m.fit(pairs.data_ptr(), n, epochs=3, batch=8192, lr=2e-3, seed=1001)
+    return m
+
+
+def member_params(c1, nf, m):
+    p = c1["params"].copy()
+    p["n_ch"] *= nf[m]
+    p["ncc"] *= nf[m]
+    return p
+
+
+def test_c1(c1):
+    args = (c1["topo"], c1["params"], c1["qlat"], c1["q0"], c1["d0"], c1["rl0"])
+    g = T.route_tree(*args, cfg=cfg_of(REF))
+    e = max_rel(g["q"], oracle(c1, c1["params"], c1["qlat"], REF, 0)["q"])
+    report("c1", REF, "libm", e)
+    assert e < 1e-10
+    g = T.route_tree(*args, cfg=cfg_of(TIGHT))
+    o1 = oracle(c1, c1["params"], c1["qlat"], TIGHT, 1)
+    report("c1", TIGHT, "crpow", max_rel(g["q"], o1["q"]))
+    np.testing.assert_array_equal(g["q"], o1["q"])
+    np.testing.assert_array_equal(g["d"], o1["d"])
+    assert g["stats"]["iterations"] == o1["iterations"]
+    report("c1", TIGHT, "libm", max_rel(g["q"], oracle(c1, c1["params"], c1["qlat"], TIGHT, 0)["q"]))
+
+
+def test_c2():
+    nets = synth.basins(seed=1002, n_trees=256)
+    S = sum(n["topo"]["n_segments"] for n in nets)
+    qlat = synth.make_qlat(1002, S, 1)
+    for tol, modes in ((REF, (0,)), (TIGHT, (1,))):
+        with T.Network([n["topo"] for n in nets], [n["params"] for n in nets], cfg=cfg_of(tol)) as b:
+            b.set_state(np.full(S, synth.Q0), np.full(S, synth.D0),
+                        np.concatenate([np.full(len(n["topo"]["reach_seg_start"]), synth.Q0) for n in nets]))
+            b.run(qlat)
+            q = b.get_state()[0]
+        for mode in modes:
+            worst, off = 0.0, 0
+            for n in nets:
+                Sn = n["topo"]["n_segments"]
+                net = dict(n, q0=np.full(Sn, synth.Q0), d0=np.full(Sn, synth.D0),
+                           rl0=np.full(len(n["topo"]["reach_seg_start"]), synth.Q0))
+                o = oracle(net, n["params"], np.ascontiguousarray(qlat[:, off:off + Sn]), tol, mode)
+                worst = max(worst, max_rel(q[off:off + Sn], o["q"]))
+                if tol is TIGHT and mode == 1:
+                    np.testing.assert_array_equal(q[off:off + Sn], o["q"])
+                off += Sn
+            report("c2", tol, "libm" if mode == 0 else "crpow", worst)
+            if tol is REF:
+                assert worst < 1e-10
+
+
+def test_c4(c1, members):
+    qf, nf = members
+    S = c1["topo"]["n_segments"]
+    M = 64
+    for tol, modes in ((REF, (0,)), (TIGHT, (1,))):
+        with T.Network.ensemble(c1["topo"], c1["params"], M, n_scale=nf, qlat_scale=qf, cfg=cfg_of(tol)) as net:
+            net.set_state(np.tile(c1["q0"], M), np.tile(c1["d0"], M), np.tile(c1["rl0"], M))
+            net.run(c1["qlat"][:1])
+            q = net.get_state()[0]
+        for mode in modes:
+            worst = 0.0
+            for m in MEMBERS:
+                o = oracle(c1, member_params(c1, nf, m), c1["qlat"][:1] * qf[m][None, :], tol, mode)
+                worst = max(worst, max_rel(q[m * S:(m + 1) * S], o["q"]))
+                if tol is TIGHT and mode == 1:
+                    np.testing.assert_array_equal(q[m * S:(m + 1) * S], o["q"])
+            report(f"c4 members {MEMBERS}", tol, "libm" if mode == 0 else "crpow", worst)
+            if tol is REF:
+                assert worst < 1e-10
+
+
+def test_c4w_warm_start_replays(c1, members, model):
+    qf, nf = members
+    S = c1["topo"]["n_segments"]
+    M = 64
+    cfg = cfg_of(TIGHT, warm_start=1, warm_k=16, record_start=1)
+    with T.Network.ensemble(c1["topo"], c1["params"], M, n_scale=nf, qlat_scale=qf, cfg=cfg) as net:
+        net.set_warm_start(model, 0.05)
+        net.set_state(np.tile(c1["q0"], M), np.tile(c1["d0"], M), np.tile(c1["rl0"], M))
+        st = net.run(c1["qlat"][:1])
+        start = net.start_history(1)
+        q = net.get_state()[0]
+    assert st["warm_used"] > 0.9 * (st["solves"] - st["early_exits"])
+    worst = 0.0
+    for m in MEMBERS:
+        o = oracle(c1, member_params(c1, nf, m), c1["qlat"][:1] * qf[m][None, :], TIGHT, 1,
+                   warm_start=np.ascontiguousarray(start[:, m * S:(m + 1) * S]), warm_delta=0.05, warm_k=16)
+        worst = max(worst, max_rel(q[m * S:(m + 1) * S], o["q"]))
+        np.testing.assert_array_equal(q[m * S:(m + 1) * S], o["q"])
+    report(f"c4w members {MEMBERS}", TIGHT, "crpow warm replay", worst)
+
+
+def test_c3_fresh_network_warm_start_replays(model):
+    w = synth.network("c1", seed=2001, n_ts=1)
+    cfg = cfg_of(TIGHT, warm_start=1, warm_k=16, record_start=1)
+    with T.Network(w["topo"], w["params"], cfg=cfg) as net:
+        net.set_warm_start(model, 0.05)
+        net.set_state(w["q0"], w["d0"], w["rl0"])
+        net.run(w["qlat"])
+        start = net.start_history(1)
+        q = net.get_state()[0]
+    o = oracle(w, w["params"], w["qlat"], TIGHT, 1, warm_start=start, warm_delta=0.05, warm_k=16)
+    report("c3", TIGHT, "crpow warm replay", max_rel(q, o["q"]))
+    np.testing.assert_array_equal(q, o["q"])
