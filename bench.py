@@ -10,9 +10,10 @@ Default workload c4w (the combined form): a 64-member ensemble over the
 inflow x LogN(0, 0.3) and Manning's n x U(0.8, 1.2) per member -- routed in one
 persistent launch with the learned warm start, FP64 state. The MLP is trained
 in the same run, untimed, on (input, converged depth) pairs of an 18-step
-plain run of the single network (~49M pairs). One bench "step" = 16 routed
-time steps of all 64 members (2.8G segment-steps), replayed from a captured
-CUDA graph, the state carrying over. Beside it, in the same run, the plain
+plain run of the single network (~49M pairs). One bench "step" = 32 routed
+time steps of all 64 members (5.5G segment-steps) in one persistent launch
+(longer launches amortise the dependency graph's fill and drain), replayed
+from a captured CUDA graph, the state carrying over; 3 timed after 3 warm-up. Beside it, in the same run, the plain
 single-basin routing of the same network (144 steps per graph launch) is
 timed: `plain_single_basin`, and `speedup_vs_plain` = value / that.
 
@@ -59,7 +60,7 @@ BYTES_PER_SEG_STEP = 112  # params 64 + qlat 8 + q 8 + depth 8 read; q, depth, v
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c4w")
@@ -192,7 +193,7 @@ def workload(name: str, n_ts: int | None, all_members: bool = True):
     """Single networks ('c1', 'c0', 'tree:<segments>', 'c3' = fresh-seed c1
     with warm start) or the batched forms: 'c2' (256 basins with
     LogU(500, 200,000) segments, 288 steps), 'c4' / 'c4w' (64 ensemble
-    members of the c1 network, without / with warm start; 16 steps per bench
+    members of the c1 network, without / with warm start; 32 steps per bench
     step)."""
     from troute_gb300 import synth
 
@@ -215,7 +216,7 @@ def workload(name: str, n_ts: int | None, all_members: bool = True):
             M, base_net = int(parts[1]), f"tree:{int(parts[2])}"
         else:
             M, base_net = 64, "c1"
-        T = 16 if n_ts is None else n_ts
+        T = 32 if n_ts is None else n_ts
         w = synth.network(base_net, n_ts=T)
         w["base"] = base_net
         S = w["topo"]["n_segments"]
