@@ -1,8 +1,9 @@
 /*
  * CPU oracle for the t-route Muskingum-Cunge secant routing path.
  *
- * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
- * CPU legs of bench.py as the checker. Nothing in the product calls it.
+ * TEST INFRASTRUCTURE ONLY: the reference's algorithm that tests/,
+ * __graft_entry__.smoke() and the CPU legs of bench.py compare the CUDA path
+ * with. Nothing in the product calls it.
  *
  * This is a plain-C restatement of the reference's FP64 CPU routines:
  *   - oracle_mc_solve  follows cpu_mc's inlined solve,
@@ -16,7 +17,7 @@
  * maxiter, attempts) are parameters; at rtol = atol = 0.01, maxiter = 100,
  * attempts = 5 the arithmetic is operation-for-operation the reference's
  * (same association order, no FMA contraction: build with -ffp-contract=off),
- * which tests/test_oracle_ref.py checks bit-for-bit against the compiled
+ * which tests/test_oracle.py checks bit-for-bit against the compiled
  * reference.
  */
 #include "troute_oracle.h"

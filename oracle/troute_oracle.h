@@ -1,15 +1,16 @@
 /*
  * CPU oracle for the t-route Muskingum-Cunge secant routing path.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker that the CUDA path is
- * compared against; it is called only by tests/, by __graft_entry__.smoke() and
- * by bench.py's CPU-baseline / reference legs. The product (libtroute_gb300.so
+ * TEST INFRASTRUCTURE ONLY. This library is the restated reference algorithm
+ * that the CUDA path is compared against; it is called only by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline / reference legs. The product (libtroute_gb300.so
  * and the troute_gb300 Python package) never links, loads or calls it.
  *
- * Pinned against the reference itself: tests/test_oracle_ref.py compiles the
+ * Pinned against the reference itself: tests/test_oracle.py loads the
  * reference's own cpu_mc (water-prediction/t-route/troute_mc_final.cu:167-252)
  * and cpu_wavefront_fp64 (water-prediction/t-route/wavefront/wavefront_mc.cu:
- * 495-564) and checks this restatement bit-for-bit at the reference tolerance;
+ * 495-564), compiled from the reference's sources by oracle/Makefile, and
+ * checks this restatement bit-for-bit at the reference tolerance;
  * tests/golden/ holds fixtures produced by those compiled reference routines.
  */
 #ifndef TROUTE_ORACLE_H

@@ -2,7 +2,8 @@
 reference routines.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU legs of bench.py as the checker. The product package never imports it.
+CPU legs of bench.py, which compare the CUDA path with it. The product package
+never imports it.
 
   oracle_cpu_mc / oracle_route_tree   our C restatement (troute_oracle.c),
       built into oracle/_build/libtroute_oracle.so by `make -C oracle oracle`;
