@@ -80,7 +80,7 @@ typedef struct troute_stats {
     unsigned long long warm_used;     /* solves that started from the learned depth */
     unsigned long long warm_fallback; /* warm-started solves that fell back to the plain secant */
     unsigned long long iter_hist[16]; /* iterations per solve, last bin = 15+ */
-    unsigned long long warp_passes;   /* passes of the per-lane refill loop (mapping 2) */
+    unsigned long long warp_passes;   /* loop passes of the per-lane kernels' warps (mappings 2, 3) */
     unsigned long long lane_busy;     /* lane-passes spent evaluating a depth */
     unsigned long long lane_wait;     /* lane-passes waiting for inputs */
     unsigned long long lane_idle;     /* lane-passes with no work */
