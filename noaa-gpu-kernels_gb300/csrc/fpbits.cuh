@@ -173,4 +173,16 @@ __device__ __forceinline__ bool quot_gt_pos(double a, double b, double c)
 // |x| on the integer pipe
 __device__ __forceinline__ double fp_abs(double x) { return __longlong_as_double(dbits(x) & 0x7fffffffffffffffll); }
 
+// x is finite (not infinite, not NaN)
+__device__ __forceinline__ bool fp_finite(double x) { return (dbits(x) & kInfBits) != kInfBits; }
+
+// 0.5 * x: for an exponent field of 2..0x7fe the product is x with the field
+// lowered by one, exactly (the result stays normal); zeros, subnormals,
+// the smallest normals, infinities and NaN take the multiplication.
+__device__ __forceinline__ double fp_half(double x)
+{
+    const unsigned e = (unsigned)((unsigned long long)dbits(x) >> 52) & 0x7ffu;
+    return (e - 2u < 0x7fdu) ? __longlong_as_double(dbits(x) - (1ll << 52)) : 0.5 * x;
+}
+
 }  // namespace tr

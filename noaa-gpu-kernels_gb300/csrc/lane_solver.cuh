@@ -132,6 +132,7 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
 {
     const Tol& tol = run.tol;
     const double dt = run.dt;
+    const double dt2 = run.dt_half;  // dt / 2 (exact), formed on the host
     if (L.mode == L_SOLVE && L.warm != W_PENDING) {
         // the segment's parameters, staged in shared memory when the solve began
         const SegP p = staged_seg(slot);
@@ -149,13 +150,26 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
         }
         const double A = (p.bw + below * p.z) * below;
         const double WP = p.bw + below * p.sq2;  // bw + 2 below sqrt(1+z^2)
-        const double AC = p.twcc * above;
-        const double WPC = fp_gt0(above) ? (p.twcc + 2.0 * above) : 0.0;
-        const double P = WP + WPC;
+        // the compound-channel terms: area A + AC, wetted perimeter P = WP + WPC,
+        // conveyance weight WP n + WPC ncc
+        double AAC, P, WPn;
+        if (fp_gt0(above) || !fp_finite(p.twcc) || !fp_finite(p.ncc)) {
+            const double AC = p.twcc * above;
+            const double WPC = fp_gt0(above) ? (p.twcc + 2.0 * above) : 0.0;
+            AAC = A + AC;
+            P = WP + WPC;
+            WPn = WP * p.n_ch + WPC * p.ncc;
+        } else {
+            // in bank (above = +0) with finite twcc, ncc: AC = +-0 and WPC = 0,
+            // and adding a zero to A >= +0, WP > 0 or WP n > 0 returns it unchanged
+            AAC = A;
+            P = WP;
+            WPn = WP * p.n_ch;
+        }
         const bool P_pos = fp_gt0(P);
         // the two quotients by P share one correctly rounded reciprocal
         const SharedRcp rP = shared_rcp(P_pos ? P : 1.0);
-        const double R = P_pos ? shared_div(A + AC, rP) : 0.0;
+        const double R = P_pos ? shared_div(AAC, rP) : 0.0;
         double r23, r53;
         pow23_53(R, &r23, &r53);
         {
@@ -166,7 +180,7 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
             e.Km = fp_gt0(e.Ck) ? fp_max_pos(dt, p.dx / e.Ck) : dt;
             e.twu = (fp_gt_pos(x, p.bfd) && twcc_pos) ? p.twcc : twl;
             // 1.0 / t is the correctly rounded reciprocal of t
-            e.Qmn = P_pos ? __drcp_rn(shared_div(WP * p.n_ch + WPC * p.ncc, rP)) * (A + AC) * r23 * p.sq_s0 : 0.0;
+            e.Qmn = P_pos ? __drcp_rn(shared_div(WPn, rP)) * AAC * r23 * p.sq_s0 : 0.0;
             if (L.need0) {
                 L.e0 = e;
                 L.need0 = 0;
@@ -178,14 +192,14 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                 {
                     const double g1 = e0.twu * p.s0, g2 = g1 * e0.Ck, g = g2 * p.dx;
                     if (fp_gt0(e0.Ck) && fp_gt0(g))
-                        X0 = fp_min_pos(0.5, fp_max0(0.5 * (1.0 - L.Qj_0 / twice_chain(g1, g2, g, e0.twu, p.s0, e0.Ck, p.dx))));
+                        X0 = fp_min_pos(0.5, fp_max0(fp_half(1.0 - L.Qj_0 / twice_chain(g1, g2, g, e0.twu, p.s0, e0.Ck, p.dx))));
                 }
-                double D0 = e0.Km * (1.0 - X0) + dt / 2.0;
+                double D0 = e0.Km * (1.0 - X0) + dt2;
                 if (fp_eq0(D0)) D0 = 1.0;
                 const SharedRcp r0 = shared_rcp(D0);
-                const double c1 = shared_div(e0.Km * X0 + dt / 2.0, r0);
-                const double c2 = shared_div(dt / 2.0 - e0.Km * X0, r0);
-                const double c3 = shared_div(e0.Km * (1.0 - X0) - dt / 2.0, r0);
+                const double c1 = shared_div(e0.Km * X0 + dt2, r0);
+                const double c2 = shared_div(dt2 - e0.Km * X0, r0);
+                const double c3 = shared_div(e0.Km * (1.0 - X0) - dt2, r0);
                 const double c4 = shared_div(ql * dt, r0);
                 const double qmc0 = c1 * qup + c2 * quc + c3 * qdp + c4;
                 L.Qj_0 = qmc0 - e0.Qmn;
@@ -194,14 +208,14 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                 {
                     const double g1 = e.twu * p.s0, g2 = g1 * e.Ck, g = g2 * p.dx;
                     if (fp_gt0(e.Ck) && fp_gt0(g))
-                        X = fp_min_pos(0.5, fp_max_pos(0.25, 0.5 * (1.0 - qmc0 / twice_chain(g1, g2, g, e.twu, p.s0, e.Ck, p.dx))));
+                        X = fp_min_pos(0.5, fp_max_pos(0.25, fp_half(1.0 - qmc0 / twice_chain(g1, g2, g, e.twu, p.s0, e.Ck, p.dx))));
                 }
-                double D1 = e.Km * (1.0 - X) + dt / 2.0;
+                double D1 = e.Km * (1.0 - X) + dt2;
                 if (fp_eq0(D1)) D1 = 1.0;
                 const SharedRcp r1 = shared_rcp(D1);
-                const double C1 = shared_div(e.Km * X + dt / 2.0, r1);
-                const double C2 = shared_div(dt / 2.0 - e.Km * X, r1);
-                const double C3 = shared_div(e.Km * (1.0 - X) - dt / 2.0, r1);
+                const double C1 = shared_div(e.Km * X + dt2, r1);
+                const double C2 = shared_div(dt2 - e.Km * X, r1);
+                const double C3 = shared_div(e.Km * (1.0 - X) - dt2, r1);
                 double C4 = shared_div(ql * dt, r1);
                 const double S3 = C1 * qup + C2 * quc + C3 * qdp;
                 if (fp_lt0(C4) && fp_abs_gt(C4, S3)) C4 = -S3;

@@ -857,6 +857,7 @@ static int enqueue_chunk(troute_handle* H, const double* qlat_dev, int n_ts, con
     run.step_base = H->step_base.p;
     run.n_ts = n_ts;
     run.dt = H->dt;
+    run.dt_half = H->dt / 2.0;
     run.qlat = qlat_dev;
     run.qlat_ld = H->qlat_cols;
     run.wave_ptr = wave;

@@ -106,6 +106,7 @@ struct RunDev {
     const int* step_base;    // device: cumulative steps before this run
     int n_ts;
     double dt;
+    double dt_half;          // dt / 2.0
     const double* qlat;      // [n_ts][qlat_ld]
     long long qlat_ld;
     const unsigned long long* wave_ptr;  // [n_ts + n_levels] ticket prefix per wave
