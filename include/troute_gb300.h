@@ -399,7 +399,9 @@ typedef struct troute_netfile {
  * TROUTE_EIO / TROUTE_ETOPO; the reference's reader exits or reads short). */
 int troute_read_network(const char* dir, troute_netfile** net);
 void troute_free_network(troute_netfile* net);
-/* Writes the three files (byte-compatible with the reference's writer). */
+/* Writes the three files (byte-compatible with the reference's writer).
+ * With qlat, qup0, qdp0 and dp0 all NULL (and n_ts 0) only topo.bin and
+ * params.bin are written, as the reference's GeoPackage parser does. */
 int troute_write_network(const char* dir, const troute_netfile* net);
 
 /* ---- lateral-inflow pre-processor -------------------------------------- */

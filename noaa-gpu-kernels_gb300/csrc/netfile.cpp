@@ -251,6 +251,12 @@ extern "C" int troute_write_network(const char* dir, const troute_netfile* n)
         if ((rc = open_file(F, dir, "params.bin", "wb"))) return rc;
         if ((rc = write_exact(F, n->params, sizeof(troute_chparams_f32), S))) return rc;
     }
+    // without initial state and inflow (the GeoPackage ingest's output) only
+    // the topology and the parameters are written
+    if (!n->qlat && !n->qup0 && !n->qdp0 && !n->dp0) {
+        if (n->n_ts != 0) return set_error(TROUTE_EINVAL, "n_ts > 0 without lateral inflow");
+        return TROUTE_OK;
+    }
     {
         File F;
         if ((rc = open_file(F, dir, "forcings.bin", "wb"))) return rc;

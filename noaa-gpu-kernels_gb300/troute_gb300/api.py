@@ -581,7 +581,8 @@ def read_network(path: str) -> dict:
 
 
 def write_network(path: str, net: dict):
-    """Writes a dict as returned by read_network as the reference's three files."""
+    """Writes a dict as returned by read_network as the reference's three files
+    (topo.bin and params.bin only when the dict has no "qlat")."""
     keep = {}
 
     def arr(k, dt):
@@ -591,7 +592,8 @@ def write_network(path: str, net: dict):
 
     n = NetFile()
     n.n_reaches, n.n_segments, n.n_levels = int(net["n_reaches"]), int(net["n_segments"]), int(net["n_levels"])
-    n.max_upstream, n.n_ts = int(net["max_upstream"]), int(net["qlat"].shape[0])
+    has_forcings = net.get("qlat") is not None
+    n.max_upstream, n.n_ts = int(net["max_upstream"]), int(net["qlat"].shape[0]) if has_forcings else 0
     for k in _NET_INT:
         setattr(n, k, arr(k, np.int32))
     p = np.ascontiguousarray(net["params"])
@@ -599,8 +601,9 @@ def write_network(path: str, net: dict):
         p = np.ascontiguousarray(np.asarray(p, np.float32).reshape(-1, 8)).view(CHPARAMS_F32_DTYPE).reshape(-1)
     keep["params"] = p
     n.params = p.ctypes.data_as(C.c_void_p)
-    for k in ("qlat", "qup0", "qdp0", "dp0"):
-        setattr(n, k, arr(k, np.float32))
+    if has_forcings:
+        for k in ("qlat", "qup0", "qdp0", "dp0"):
+            setattr(n, k, arr(k, np.float32))
     os.makedirs(path, exist_ok=True)
     _check(lib().troute_write_network(os.fsencode(path), C.byref(n)))
 
