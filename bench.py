@@ -13,9 +13,10 @@ in the same run, untimed, on (input, converged depth) pairs of an 18-step
 plain run of the single network (~49M pairs). One bench "step" = 32 routed
 time steps of all 64 members (5.5G segment-steps) in one persistent launch
 (longer launches amortise the dependency graph's fill and drain), replayed
-from a captured CUDA graph, the state carrying over; 3 timed after 3 warm-up. Beside it, in the same run, the plain
-single-basin routing of the same network (144 steps per graph launch) is
-timed: `plain_single_basin`, and `speedup_vs_plain` = value / that.
+from a captured CUDA graph, the state carrying over; 3 timed after 3
+warm-up. Beside it, in the same run, the plain single-basin routing of the
+same network (144 steps per graph launch) is timed: `plain_single_basin`,
+and `speedup_vs_plain` = value / that.
 
 Other workloads: c1 (plain single basin, 144 steps per bench step), c0, c2
 (256 uneven basins), c3 (warm start on a fresh-seed c1 network, trained on
@@ -37,6 +38,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -334,6 +336,27 @@ def single_network(w) -> tuple:
     return w["topo"], w["params"], w["qlat"], w["q0"], w["d0"], w["rl0"], "the"
 
 
+def host_cpu() -> dict:
+    """The host the CPU legs ran on: hardware threads and the CPU model."""
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                key = ln.split(":", 1)[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if not model:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            model = next((ln.split(":", 1)[1].strip() for ln in out.splitlines() if ln.startswith("Model name")), "")
+        except (OSError, subprocess.SubprocessError):
+            model = ""
+    return {"nproc": os.cpu_count() or 1, "cpu_model": model or platform.machine()}
+
+
 def cpu_baseline(w) -> dict:
     """The oracle port of cpu_wavefront_fp64, one core, one routed step of the
     same network from its initial state (plain secant start, the reference's)."""
@@ -348,7 +371,7 @@ def cpu_baseline(w) -> dict:
     dt = time.perf_counter() - t0
     return {"value": S / dt, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"1 routed step of {label} {S}-segment network from its initial state, rtol 1e-8, "
-                      f"single thread ({dt:.1f} s)"}
+                      f"single thread ({dt:.1f} s)", "host": host_cpu()}
 
 
 # --------------------------------------------------------------------------- reference arm
@@ -390,7 +413,8 @@ def run_reference(args, dist: Dist):
                                    f"start (the reference's); one routed step per bench step", "segments": S},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
                              "sample": f"1 routed time step of {label} {S}-segment network per bench step, "
-                                       f"{nth} threads (level-parallel oracle port of cpu_wavefront_fp64)"},
+                                       f"{nth} threads (level-parallel oracle port of cpu_wavefront_fp64)",
+                             "host": host_cpu()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

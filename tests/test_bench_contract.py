@@ -23,5 +23,6 @@ def test_reference_arm_line():
     assert line["unit"] == "seg-steps/s" and line["dtype"] == "f64"
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    assert cb["host"]["nproc"] >= cb["cores"] and cb["host"]["cpu_model"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
