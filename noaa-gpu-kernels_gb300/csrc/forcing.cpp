@@ -10,23 +10,28 @@
 //    and value = atof(text after the last comma); rows with a step outside
 //    [0, n_ts) are ignored, later rows of a file overwrite earlier ones (so a
 //    header line, read as step 0, is overwritten by the real step-0 row).
-// Files are handed to threads in directory order in contiguous chunks; each
-// file's cells belong to one reach, so the result does not depend on the
-// thread count.
+// The directory is listed once (ids looked up there); the files are handed to
+// threads in directory order in contiguous chunks. Each file's cells belong
+// to one reach, so the result does not depend on the thread count (unless two
+// files name the same id, e.g. nex-12 and nex-012: then, as in the reference
+// tool, the one written last wins).
+#include <dirent.h>
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <atomic>
+#include <cerrno>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <filesystem>
 #include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
 
 #include "troute_internal.h"
-
-namespace fs = std::filesystem;
 
 namespace {
 
@@ -74,44 +79,69 @@ extern "C" int troute_qlat_from_csv(const char* csv_dir, const int64_t* reach_id
     std::unordered_map<int64_t, int> index;
     index.reserve((size_t)n_reaches * 2);
     for (int i = 0; i < n_reaches; ++i) index[reach_ids[i]] = i;  // a repeated id maps to its last reach
-    std::vector<std::string> paths;
-    std::error_code ec;
-    for (fs::directory_iterator it(csv_dir, ec), end; !ec && it != end; it.increment(ec)) {
-        if (!it->is_regular_file(ec)) continue;
-        const std::string name = it->path().filename().string();
-        if (name.rfind("nex-", 0) != 0 || name.find("_output.csv") == std::string::npos) continue;
-        paths.push_back(it->path().string());
+    // one pass over the directory: the output files and their reaches (the id
+    // lookup is done here, once, so the workers only open, read and parse)
+    struct CsvFile {
+        std::string name;
+        int reach;
+    };
+    std::vector<CsvFile> files;
+    long long n_unknown = 0;
+    DIR* dir = opendir(csv_dir);
+    if (!dir) return set_error(TROUTE_EIO, "cannot list %s: %s", csv_dir, std::strerror(errno));
+    const int dfd = dirfd(dir);
+    errno = 0;
+    for (const dirent* e; (e = readdir(dir)) != nullptr; errno = 0) {
+        const char* nm = e->d_name;
+        if (std::strncmp(nm, "nex-", 4) != 0 || !std::strstr(nm, "_output.csv")) continue;
+        bool regular = e->d_type == DT_REG;
+        if (e->d_type == DT_UNKNOWN || e->d_type == DT_LNK) {
+            struct stat st;
+            regular = fstatat(dfd, nm, &st, 0) == 0 && S_ISREG(st.st_mode);
+        }
+        if (!regular) continue;
+        const long long id = file_id(nm);
+        const auto hit = id < 0 ? index.end() : index.find((int64_t)id);
+        if (hit == index.end()) {
+            ++n_unknown;
+            continue;
+        }
+        files.push_back({nm, hit->second});
     }
-    if (ec) return set_error(TROUTE_EIO, "cannot list %s: %s", csv_dir, ec.message().c_str());
+    if (errno != 0) {
+        const int err = errno;
+        closedir(dir);
+        return set_error(TROUTE_EIO, "cannot list %s: %s", csv_dir, std::strerror(err));
+    }
     if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
-    std::atomic<long long> n_match{0}, n_miss{0};
+    std::atomic<long long> n_match{0}, n_miss{n_unknown};
     std::atomic<int> io_error{0};
-    const size_t per = (paths.size() + (size_t)n_threads - 1) / (size_t)n_threads;
+    const size_t per = (files.size() + (size_t)n_threads - 1) / (size_t)n_threads;
     auto work = [&](size_t b, size_t e) {
-        std::vector<char> buf(4096);
-        for (size_t pi = b; pi < e; ++pi) {
-            const long long id = file_id(fs::path(paths[pi]).filename().string());
-            const auto hit = id < 0 ? index.end() : index.find((int64_t)id);
-            if (hit == index.end()) {
-                n_miss.fetch_add(1);
-                continue;
-            }
-            const int reach = hit->second;
-            FILE* fp = std::fopen(paths[pi].c_str(), "rb");
-            if (!fp) {
+        std::vector<char> buf(8192);
+        for (size_t fi = b; fi < e; ++fi) {
+            const int fd = openat(dfd, files[fi].name.c_str(), O_RDONLY | O_CLOEXEC);
+            if (fd < 0) {
                 n_miss.fetch_add(1);
                 continue;
             }
             size_t got = 0;
+            bool failed = false;
             while (true) {
                 if (buf.size() < got + 4097) buf.resize(std::max(buf.size() * 2, got + 4097));
-                const size_t k = std::fread(buf.data() + got, 1, 4096, fp);
-                got += k;
-                if (k < 4096) break;
+                const ssize_t k = read(fd, buf.data() + got, buf.size() - 1 - got);
+                if (k < 0) {
+                    if (errno == EINTR) continue;
+                    failed = true;
+                    break;
+                }
+                if (k == 0) break;
+                got += (size_t)k;
             }
-            if (std::ferror(fp)) io_error.store(1);
-            std::fclose(fp);
+            close(fd);
+            if (failed) io_error.store(1);
             buf[got] = 0;
+            const int reach = files[fi].reach;
             size_t i = 0;
             while (i < got) {
                 const size_t ls = i;
@@ -129,11 +159,12 @@ extern "C" int troute_qlat_from_csv(const char* csv_dir, const int64_t* reach_id
     };
     std::vector<std::thread> pool;
     for (int t = 0; t < n_threads; ++t) {
-        const size_t b = (size_t)t * per, e = std::min(b + per, paths.size());
+        const size_t b = (size_t)t * per, e = std::min(b + per, files.size());
         if (b >= e) break;
         pool.emplace_back(work, b, e);
     }
     for (auto& th : pool) th.join();
+    closedir(dir);
     if (matched) *matched = n_match.load();
     if (missing) *missing = n_miss.load();
     if (io_error.load()) return set_error(TROUTE_EIO, "read error in %s", csv_dir);
