@@ -336,6 +336,20 @@ def single_network(w) -> tuple:
     return w["topo"], w["params"], w["qlat"], w["q0"], w["d0"], w["rl0"], "the"
 
 
+def topology_bytes_per_seg_step(w) -> float:
+    """Reach-topology bytes a step reads per segment, beside the algorithmic
+    112 B: per reach its segment range, upstream CSR row and downstream index
+    (16 B), per upstream link 4 B."""
+    if "batch" in w:
+        topos = [n["topo"] for n in w["batch"]]
+    else:
+        topos = [w["topo"]] * int(w.get("members", 1))
+    R = sum(len(t["reach_seg_start"]) for t in topos)
+    links = sum(len(t["reach_up_idx"]) for t in topos)
+    S = sum(int(t["n_segments"]) for t in topos)
+    return (16.0 * R + 4.0 * links) / max(1, S)
+
+
 def host_cpu() -> dict:
     """The host the CPU legs ran on: hardware threads and the CPU model."""
     model = ""
@@ -497,6 +511,8 @@ def run_ours(args, dist: Dist):
     tr, tr_src = profiled("dram_bytes_per_seg_step", bool(model))
     fp64, _ = profiled("fp64_pipe_active_pct", bool(model))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "alg_bytes_per_seg_step": BYTES_PER_SEG_STEP,
+                "topology_bytes_per_seg_step": topology_bytes_per_seg_step(w),
                 "traffic": (tr * seg_steps if tr is not None else None),
                 "traffic_source": f"profiles/{tr_src} (DRAM bytes per segment-step x segment-steps of a launch)",
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
