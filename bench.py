@@ -177,10 +177,8 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profiled(key: str, warm: bool):
-    """A figure of the routing kernel from the committed ncu summary: the
-    warm-started kernel's (an ensemble capture) or the plain kernel's."""
-    name = "route_dataflow_warm_ens256.md" if warm else "route_kernel_c1.md"
+def profiled_file(key: str, name: str):
+    """A `key: value` figure from a committed ncu summary under profiles/."""
     p = os.path.join(ROOT, "profiles", name)
     try:
         for ln in open(p):
@@ -189,6 +187,33 @@ def profiled(key: str, warm: bool):
     except OSError:
         pass
     return None, name
+
+
+def profiled(key: str, warm: bool):
+    """A figure of the routing kernel from the committed ncu summary: the
+    warm-started kernel's (an ensemble capture) or the plain kernel's."""
+    return profiled_file(key, "route_dataflow_warm_ens256.md" if warm else "route_kernel_c1.md")
+
+
+def critical_path_bound(T, w, n_ts: int, it_per_solve: float, sm_mhz, kernel_ms: float) -> dict:
+    """The dependency graph's critical path of one bench step set against the
+    FP64 pipe: the longest chain of segment solves (troute_critical_path), each
+    solve at least (iterations + 1) passes, each pass at least its FP64 warp
+    instructions x 64 cycles (one FP64 warp instruction per 64 cycles per
+    SMSP, however few lanes are busy)."""
+    if "batch" in w:
+        chain = max(T.critical_path(n["topo"], n_ts) for n in w["batch"])
+    else:
+        chain = T.critical_path(w["topo"], n_ts)
+    out = {"segment_solves": chain, "passes_per_solve": it_per_solve + 1.0}
+    instr, src = profiled_file("fp64_instr_per_solving_pass", "route_dataflow_instmix_tree200k.md")
+    if instr is None:
+        return out
+    pass_us = instr * 64.0 / float(sm_mhz or 2070.0)
+    bound_ms = chain * (it_per_solve + 1.0) * pass_us / 1e3
+    out.update({"fp64_instr_per_pass": instr, "instr_source": f"profiles/{src}", "pass_us_min": pass_us,
+                "lower_bound_ms": bound_ms, "kernel_ms": kernel_ms, "kernel_over_bound": kernel_ms / bound_ms})
+    return out
 
 
 def workload(name: str, n_ts: int | None, all_members: bool = True):
@@ -555,6 +580,7 @@ def run_ours(args, dist: Dist):
     if dist.rank == 0 and not args.no_cpu_baseline and "topo" in w:
         cpu = cpu_baseline(w)
     it = stats["iterations"]
+    crit = critical_path_bound(T, w, n_ts, it / max(1, stats["solves"]), clocks.get("sm_mhz"), kernel_ms)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
@@ -565,7 +591,7 @@ def run_ours(args, dist: Dist):
                        "l2": f"inputs larger than L2 (129 MB): lateral inflow {w['qlat'].nbytes / 1e9:.2f} GB and "
                              f"segment parameters {S * 96 / 1e9:.2f} GB read per bench step",
                        "parallelism": "replicas" if dist.world > 1 else "single GPU"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "roofline": roofline, "critical_path": crit, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": 4 * args.steps,
             "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
                        "early_exits": stats["early_exits"], "warm_used": stats["warm_used"],

@@ -324,6 +324,12 @@ int troute_debug_div(const double* a, const double* b, int n, double* out);
 int troute_debug_quot_gt(const double* a, const double* b, double c, int n, int* out);
 
 /* ---- schedule and topology helpers ----------------------------------- */
+/* Longest chain of segment solves in the dependency graph of an n_ts-step
+ * run (a reach's item of step t follows its item of step t - 1 and the items
+ * of step t of its upstream reaches; an item is seg_len solves in order): the
+ * critical path that bounds a run's time from below, whatever the
+ * parallelism. No counterpart in the reference. */
+int troute_critical_path(const troute_topo* topo, int n_ts, long long* solves);
 /* Topological levels as the reference builds them (level 0 = headwater,
  * level = 1 + max upstream level; gen_network.py:219-231). level_ptr needs
  * n_reaches + 1 entries of room. */

@@ -318,6 +318,40 @@ extern "C" int troute_validate(const troute_topo* topo)
     return troute_levels(R, topo->reach_up_ptr, topo->reach_up_idx, lv.data(), lp.data(), lr.data(), &L);
 }
 
+// Longest chain of segment solves in the (reach, step) dependency graph of an
+// n_ts-step run: item (r, t) follows (r, t - 1) and every (u, t) with u
+// upstream of r, and takes seg_len[r] solves in order. Dynamic programme over
+// the steps, reaches in level order within a step:
+//   L[r] <- seg_len[r] + max(L[r] of step t - 1, max over upstream u of L[u] of step t).
+extern "C" int troute_critical_path(const troute_topo* topo, int n_ts, long long* solves)
+{
+    if (!solves) return set_error(TROUTE_EINVAL, "null argument");
+    *solves = 0;
+    if (n_ts < 0) return set_error(TROUTE_EINVAL, "negative n_ts");
+    int rc = troute_validate(topo);
+    if (rc) return rc;
+    const int R = topo->n_reaches;
+    if (R == 0 || n_ts == 0) return TROUTE_OK;
+    std::vector<int> lv(R), lp(R + 1), lr(R);
+    int L = 0;
+    if ((rc = troute_levels(R, topo->reach_up_ptr, topo->reach_up_idx, lv.data(), lp.data(), lr.data(), &L)))
+        return rc;
+    std::vector<long long> chain(R, 0);  // longest chain ending with reach r's item of the current step
+    long long best = 0;
+    for (int t = 0; t < n_ts; ++t) {
+        for (int i = 0; i < R; ++i) {  // level order: upstream reaches of this step come first
+            const int r = lr[i];
+            long long m = chain[r];     // the same reach, previous step
+            for (int k = topo->reach_up_ptr[r]; k < topo->reach_up_ptr[r + 1]; ++k)
+                m = std::max(m, chain[topo->reach_up_idx[k]]);
+            chain[r] = m + topo->reach_seg_len[r];
+            best = std::max(best, chain[r]);
+        }
+    }
+    *solves = best;
+    return TROUTE_OK;
+}
+
 // ---------------------------------------------------------------------------
 // one-shot tree routing
 // ---------------------------------------------------------------------------

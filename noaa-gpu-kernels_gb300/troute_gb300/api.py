@@ -175,6 +175,7 @@ _SIGS = {
     "troute_debug_div": ([_P, _P, _I, _P], _I),
     "troute_debug_quot_gt": ([_P, _P, C.c_double, _I, _P], _I),
     "troute_levels": ([_I, _P, _P, _P, _P, _P, _P], _I),
+    "troute_critical_path": ([_P, _I, _P], _I),
     "troute_validate": ([_P], _I),
     "troute_gen_tree": ([_U64, _I, _I, _I, _P, _P, _P, _P], _I),
     "troute_gen_params": ([_U64, _I, _P], _I),
@@ -333,6 +334,16 @@ def levels(up_ptr, up_idx):
 def validate(seg_start, seg_len, up_ptr, up_idx, n_segments):
     t, _keep = _topo_struct(seg_start, seg_len, up_ptr, up_idx, n_segments)
     _check(lib().troute_validate(C.byref(t)))
+
+
+def critical_path(topo: dict, n_ts: int) -> int:
+    """Longest chain of segment solves in the (reach, step) dependency graph
+    of an n_ts-step run (troute_critical_path)."""
+    t, _keep = _topo_struct(topo["reach_seg_start"], topo["reach_seg_len"], topo["reach_up_ptr"],
+                            topo["reach_up_idx"], topo["n_segments"])
+    out = C.c_longlong()
+    _check(lib().troute_critical_path(C.byref(t), int(n_ts), C.byref(out)))
+    return int(out.value)
 
 
 # ---------------------------------------------------------------------------

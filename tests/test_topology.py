@@ -49,3 +49,36 @@ def test_levels_match_reference_construction():
     lp2, lr2 = O.levels(t["reach_up_ptr"], t["reach_up_idx"], len(t["reach_seg_start"]))
     np.testing.assert_array_equal(lp, lp2)
     np.testing.assert_array_equal(lr, lr2)
+
+
+def _critical_path_brute(topo, n_ts):
+    """Longest path in the explicit (reach, step) graph, by memoised recursion
+    from every item backwards."""
+    import functools
+
+    R = len(topo["reach_seg_start"])
+    ups = [list(topo["reach_up_idx"][topo["reach_up_ptr"][r]:topo["reach_up_ptr"][r + 1]]) for r in range(R)]
+
+    @functools.lru_cache(maxsize=None)
+    def ending_at(r, t):
+        best = 0
+        if t > 0:
+            best = ending_at(r, t - 1)
+        for u in ups[r]:
+            best = max(best, ending_at(int(u), t))
+        return best + int(topo["reach_seg_len"][r])
+
+    return max((ending_at(r, t) for r in range(R) for t in range(n_ts)), default=0)
+
+
+def test_critical_path_matches_the_explicit_graph():
+    from troute_gb300 import synth
+
+    for seed, S, n_ts in ((1, 300, 1), (2, 500, 5), (3, 800, 12)):
+        topo = synth.network(f"tree:{S}", seed=seed, n_ts=1, with_qlat=False)["topo"]
+        assert T.critical_path(topo, n_ts) == _critical_path_brute(topo, n_ts)
+    c0 = synth.network("c0", n_ts=1, with_qlat=False)["topo"]
+    # one step: the most segments on a headwater-to-outlet path; more steps add at least one reach per step
+    one = T.critical_path(c0, 1)
+    assert one == _critical_path_brute(c0, 1)
+    assert T.critical_path(c0, 4) > one and T.critical_path(c0, 0) == 0
