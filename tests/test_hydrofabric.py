@@ -18,7 +18,7 @@ from golden_inputs import GOLDEN
 from oracle import troute_oracle as O
 
 GPKG_DIR = os.path.join(GOLDEN, "gpkg")
-REF_ROOT = os.environ.get("TROUTE_REFERENCE_ROOT", "/root/reference")
+REF_ROOT = O.REF_ROOT  # the reference checkout, where present
 
 
 def _make_gpkg():
