@@ -82,3 +82,13 @@ def test_critical_path_matches_the_explicit_graph():
     one = T.critical_path(c0, 1)
     assert one == _critical_path_brute(c0, 1)
     assert T.critical_path(c0, 4) > one and T.critical_path(c0, 0) == 0
+
+
+def test_critical_path_rejects_bad_topologies():
+    bad = {"n_segments": 3, "reach_seg_start": np.array([0, 1, 2], np.int32), "reach_seg_len": np.ones(3, np.int32),
+           "reach_up_ptr": np.array([0, 1, 2, 3], np.int32), "reach_up_idx": np.array([2, 0, 1], np.int32)}
+    with pytest.raises(T.TrouteError) as e:
+        T.critical_path(bad, 4)       # a cycle
+    assert e.value.code == 2
+    ok = dict(bad, reach_up_ptr=np.array([0, 0, 1, 2], np.int32), reach_up_idx=np.array([0, 1], np.int32))
+    assert T.critical_path(ok, 1) == 3 and T.critical_path(ok, 5) == 7   # a 3-reach chain: 3 + 1 per extra step
