@@ -26,3 +26,34 @@ def test_reference_arm_line():
     assert cb["host"]["nproc"] >= cb["cores"] and cb["host"]["cpu_model"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def _bench_module():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("bench_module", os.path.join(ROOT, "bench.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def test_line_helpers_of_the_gpu_arm():
+    """The parts of the GPU arm's line that run on the host: topology bytes,
+    the critical-path bound, the host description, the committed profile
+    figures it reads."""
+    import troute_gb300 as T
+
+    b = _bench_module()
+    for name in ("c0", "ens:3:2000:w"):
+        w = b.workload(name, 4)
+        tb = b.topology_bytes_per_seg_step(w)
+        assert 2.0 < tb < 40.0
+        cp = b.critical_path_bound(T, w, 4, 6.5, 2070.0, 100.0)
+        assert cp["segment_solves"] == T.critical_path(w["topo"], 4)
+        assert cp["passes_per_solve"] == 7.5 and cp["fp64_instr_per_pass"] > 0
+        assert abs(cp["lower_bound_ms"] - cp["segment_solves"] * 7.5 * cp["pass_us_min"] / 1e3) < 1e-9
+    for warm in (False, True):
+        for key in ("dram_bytes_per_seg_step", "fp64_pipe_active_pct"):
+            v, src = b.profiled(key, warm)
+            assert v is not None and v > 0, (key, src)
+    assert b.host_cpu()["nproc"] >= 1
