@@ -92,3 +92,15 @@ def test_bad_arguments_rejected_before_device():
     with pytest.raises(T.TrouteError) as e:
         T.mc_reach_parallel(p, [0.0], [-1], [1], [0.0], [0.0], [0.0])
     assert e.value.code == 1
+
+
+def test_makefile_builds_the_same_library(tmp_path):
+    """noaa-gpu-kernels_gb300/Makefile (the build for C callers without
+    Python) produces a library exporting every declared entry point."""
+    out = tmp_path / "libtroute_gb300.so"
+    r = subprocess.run(["make", "-C", os.path.join(ROOT, "noaa-gpu-kernels_gb300"), f"-j{os.cpu_count() or 2}",
+                        f"BUILD={tmp_path / 'obj'}", f"OUT={out}"], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    nm = subprocess.run(["nm", "-D", "--defined-only", str(out)], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r" T (troute_[a-z0-9_]+)$", nm, flags=re.M))
+    assert set(declared()) <= exported
