@@ -176,3 +176,28 @@ def test_pow_mode_changes_nothing_at_reference_tolerance():
         b = O.route_tree(*args, history=True)
     rel = np.abs(a["q_hist"] - b["q_hist"]) / np.maximum(np.abs(a["q_hist"]), 1e-300)
     assert rel.max() < 1e-10
+
+
+def test_warm_started_oracle_semantics():
+    """The oracle's warm-started solve (the restatement the GPU's warm runs
+    are replayed against): no learned depth (0) is the plain solve exactly.
+    Starting from the plain run's own converged depths, a 5 % bracket takes
+    fewer secant iterations than the plain start, but a 0.2 % bracket takes
+    more: the reference's two residuals use different X clamps, so a bracket
+    too narrow for their offset sends the secant away (and into fallbacks)."""
+    from troute_gb300 import synth
+
+    c = synth.network("tree:3000", seed=21, n_ts=6)
+    args = (c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"])
+    tight = (1e-8, 1e-10, 100, 5)
+    plain = O.route_tree(*args, tol=tight, depth_history=True)
+    S = c["topo"]["n_segments"]
+    zero = O.route_tree(*args, tol=tight, warm_start=np.zeros((6, S)), warm_delta=0.05, warm_k=16)
+    np.testing.assert_array_equal(zero["q"], plain["q"])
+    assert zero["iterations"] == plain["iterations"] and zero["warm_used"] == 0
+    wide = O.route_tree(*args, tol=tight, warm_start=plain["d_hist"], warm_delta=0.05, warm_k=16)
+    narrow = O.route_tree(*args, tol=tight, warm_start=plain["d_hist"], warm_delta=0.002, warm_k=16)
+    for w in (wide, narrow):
+        assert w["warm_used"] == S * 6 and 0 < w["warm_fallback"] < w["warm_used"]
+    assert wide["iterations"] < 0.9 * plain["iterations"] < narrow["iterations"]
+    assert narrow["warm_fallback"] > wide["warm_fallback"]
