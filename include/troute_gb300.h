@@ -129,7 +129,10 @@ int troute_mc_reach_parallel_cfg(const troute_chparams* p, const double* ql,
                                  double uq, double dt, int nr,
                                  const troute_cfg* cfg, troute_stats* stats);
 /* Device-pointer form of kernel_mc_gpu (all arrays on the device, n_segments
- * = total segments); asynchronous on `stream` (a cudaStream_t, 0 = default). */
+ * = total segments); asynchronous on `stream` (a cudaStream_t, 0 = default).
+ * A reach whose segment range lies outside [0, n_segments) is skipped (its
+ * outputs are left unwritten). A CUDA error already pending on the calling
+ * thread is reported and left pending; nothing is launched. */
 int troute_mc_reach_parallel_device(const troute_chparams* p, const double* ql,
                                     const int* rs, const int* rl,
                                     const double* qu, const double* qd, const double* dp,
@@ -138,14 +141,19 @@ int troute_mc_reach_parallel_device(const troute_chparams* p, const double* ql,
                                     const troute_cfg* cfg, void* stream);
 
 /* Same computation as troute_mc_reach_parallel_device for callers that cannot
- * allocate device memory (stream capture in progress, device memory owned by
- * another framework or pool): its only scratch, the per-block solve counters,
- * is an array compiled into the library (about 1.7 MB per GPU, held until the
- * process exits). No counterpart in the reference. At most 2,097,152 reaches per
- * call (larger calls return TROUTE_EINVAL). The first call on a device looks up
- * the array's address with that device current: make it before any stream
- * capture. Calls that overlap on the GPU share the array and race. With stats
- * non-NULL the call waits for `stream` and returns the counters. */
+ * allocate device memory where they route (a host model driver or framework
+ * that owns every device buffer through its own pool, or a hot path where an
+ * allocation would synchronise the device): its only scratch, the per-block
+ * solve counters, is an array compiled into the library (about 1.7 MB per
+ * GPU, held until the process exits). No counterpart in the reference. At most
+ * 2,097,152 reaches per call (larger calls return TROUTE_EINVAL). The first
+ * call on a device looks up the array's address with that device current;
+ * that first call should come before any stream capture. Calls that overlap
+ * on the GPU share the array and race. With stats non-NULL the call waits for
+ * `stream` and returns the counters; only then is a reach with a segment range
+ * outside [0, n_segments) reported (TROUTE_EINVAL; its outputs are left
+ * unwritten). A CUDA error already pending on the calling thread is reported
+ * and left pending; nothing is launched. */
 int troute_mc_reach_parallel_device_noalloc(const troute_chparams* p, const double* ql,
                                             const int* rs, const int* rl,
                                             const double* qu, const double* qd, const double* dp,

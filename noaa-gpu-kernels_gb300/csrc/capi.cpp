@@ -45,7 +45,58 @@ struct DevPtr {
     void* p = nullptr;
     ~DevPtr() { if (p) cudaFree(p); }
 };
+
+// Counter buffers of troute_mc_reach_parallel_device: one per (host thread,
+// device), so a thread that switches devices never hands a kernel another
+// GPU's memory, and two threads never share one. Freed when the thread exits
+// (errors ignored: at process exit the runtime may already be unloading).
+constexpr int kMaxDevices = 64;
+struct ThreadDevStats {
+    DevStats* p[kMaxDevices] = {};
+    ~ThreadDevStats()
+    {
+        int cur = -1;
+        bool any = false;
+        for (int d = 0; d < kMaxDevices; ++d) {
+            if (!p[d]) continue;
+            if (!any) {
+                any = true;
+                if (cudaGetDevice(&cur) != cudaSuccess) cur = -1;
+            }
+            if (cudaSetDevice(d) == cudaSuccess) cudaFree(p[d]);
+        }
+        if (any && cur >= 0) cudaSetDevice(cur);
+        cudaGetLastError();
+    }
+};
+thread_local ThreadDevStats t_stats;
+
+int device_stats(DevStats** out)
+{
+    int dev = 0;
+    int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= kMaxDevices) return set_error(TROUTE_EINVAL, "device %d beyond the supported range", dev);
+    if (!t_stats.p[dev] && (rc = cuda_check(cudaMalloc(&t_stats.p[dev], sizeof(DevStats)), "cudaMalloc"))) {
+        t_stats.p[dev] = nullptr;
+        return rc;
+    }
+    *out = t_stats.p[dev];
+    return TROUTE_OK;
+}
 }  // namespace
+
+namespace tr {
+// An error left pending by earlier CUDA work of the calling thread is reported
+// (and left pending) rather than consumed by this library's own launch check.
+int pending_cuda_error(const char* entry)
+{
+    const cudaError_t e = cudaPeekAtLastError();
+    if (e == cudaSuccess) return TROUTE_OK;
+    return set_error(TROUTE_ECUDA, "%s: a CUDA error was pending before the call (%s); nothing was launched", entry,
+                     cudaGetErrorString(e));
+}
+}  // namespace tr
 
 extern "C" int troute_mc_reach_parallel_device(const troute_chparams* p, const double* ql,
                                                const int* rs, const int* rl,
@@ -63,8 +114,9 @@ extern "C" int troute_mc_reach_parallel_device(const troute_chparams* p, const d
     if (cfg) c = *cfg;
     int rc = check_cfg(c);
     if (rc) return rc;
-    static thread_local DevStats* stats = nullptr;
-    if (!stats && (rc = cuda_check(cudaMalloc(&stats, sizeof(DevStats)), "cudaMalloc"))) return rc;
+    if ((rc = pending_cuda_error("troute_mc_reach_parallel_device"))) return rc;
+    DevStats* stats = nullptr;
+    if ((rc = device_stats(&stats))) return rc;
     if ((rc = cuda_check(cudaMemsetAsync(stats, 0, sizeof(DevStats), (cudaStream_t)stream), "memset"))) return rc;
     return launch_reach_parallel(p, ql, rs, rl, qu, qd, dp, qo, vo, dpo, uq, dt, nr, n_segments, make_tol(c),
                                  stats, c.threads_per_block, stream);

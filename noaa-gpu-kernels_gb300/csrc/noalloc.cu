@@ -1,24 +1,30 @@
 // Reach-parallel MC step that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc at the point where they route: code
-// that runs while a CUDA stream is being captured into a graph, code whose
-// device memory is handed out by its own pool or by a host framework (for
-// example a hydrologic model driver that owns all device buffers), or code on
-// a hot path where an allocation would synchronise the device. For them this
-// entry point runs the same per-reach solve as troute_mc_reach_parallel_device
-// but keeps its only scratch memory, the per-block solve counters, in a fixed
-// array compiled into the library. Every GPU that loads the library holds that
-// array (about 1.7 MB) until the process exits.
+// Some callers cannot call cudaMalloc at the point where they route: a host
+// model driver or framework that owns every device buffer through its own
+// pool (a stray cudaMalloc would sit outside its accounting and could fail
+// when the pool has reserved the device's memory), or a hot path where an
+// allocation would synchronise the device. For them this entry point runs the
+// same per-reach solve as troute_mc_reach_parallel_device but keeps its only
+// scratch memory, the per-block solve counters, in a fixed array compiled
+// into the library. Every GPU that loads the library holds that array (about
+// 1.7 MB) until the process exits. The caller still passes every input and
+// output array.
 //
 // Limits and behaviour:
 //  - at most kNoAllocMaxBlocks blocks of kNoAllocThreads reaches, i.e.
 //    2,097,152 reaches per call; larger calls are rejected with TROUTE_EINVAL;
 //  - the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture;
-//  - all calls share the array: calls whose kernels overlap on the GPU (other
-//    streams, other host threads) race on it. Every counter a call reads is
-//    written by that call first, so nothing left from an earlier call leaks in.
+//    (cudaGetSymbolAddress) with that device current; that first call should
+//    come before any stream capture;
+//  - all calls share the array and it keeps the last call's contents: calls
+//    whose kernels overlap on the GPU (other streams, other host threads)
+//    race on it. Every counter a call reads is written by that call first, so
+//    nothing left from an earlier call leaks in;
+//  - a reach whose segment range falls outside [0, n_segments) is skipped and
+//    its outputs are left unwritten. Only a call given `stats` waits for the
+//    GPU and can report that (TROUTE_EINVAL); without `stats` the call returns
+//    as soon as the kernels are queued and cannot see it.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -30,6 +36,7 @@ namespace tr {
 
 int check_cfg(const troute_cfg& c);
 Tol make_tol(const troute_cfg& c);
+int pending_cuda_error(const char* entry);
 
 namespace {
 
@@ -187,6 +194,7 @@ extern "C" int troute_mc_reach_parallel_device_noalloc(const troute_chparams* p,
     if (cfg) c = *cfg;
     int rc = check_cfg(c);
     if (rc) return rc;
+    if ((rc = pending_cuda_error("troute_mc_reach_parallel_device_noalloc"))) return rc;
     NoAllocPartial* part = nullptr;
     if ((rc = noalloc_scratch(&part))) return rc;
     const int nblocks = (nr + kNoAllocThreads - 1) / kNoAllocThreads;

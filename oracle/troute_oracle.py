@@ -24,7 +24,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libtroute_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libtroute_ref.so")
-REF_ROOT = os.environ.get("TROUTE_REF_ROOT", "/root/reference")
+# the reference checkout: $TROUTE_REF_ROOT, else a checkout named `reference`
+# beside this repository
+REF_ROOT = os.environ.get("TROUTE_REF_ROOT") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 CHP = np.dtype([(n, "<f8") for n in ("dx", "bw", "tw", "twcc", "n_ch", "ncc", "cs", "s0")])
 CHP32 = np.dtype([(n, "<f4") for n in ("dx", "bw", "tw", "twcc", "n_ch", "ncc", "cs", "s0")])

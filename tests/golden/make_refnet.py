@@ -68,4 +68,6 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    from oracle.troute_oracle import REF_ROOT  # $TROUTE_REF_ROOT, else ../reference beside the repository
+
+    main(sys.argv[1] if len(sys.argv) > 1 else REF_ROOT)

@@ -1,10 +1,12 @@
 """The no-allocation reach-parallel entry point.
 
-Callers that cannot allocate device memory (code running under stream
-capture, or whose device buffers belong to another framework's pool) use
+Callers that cannot allocate device memory where they route (a model driver
+whose device buffers all come from its own pool, or a hot path where an
+allocation would synchronise the device) use
 troute_mc_reach_parallel_device_noalloc, whose only scratch is an array
 compiled into the library. Through the C ABI, two calls in a row must give the
-same results as the allocating device entry point on the same device arrays.
+same results as the allocating device entry point on the same device arrays,
+and the same bits as the oracle's cpu_mc (correctly rounded powers).
 """
 import ctypes as C
 
@@ -13,6 +15,7 @@ import pytest
 
 import troute_gb300 as T
 from golden_inputs import make_golden
+from oracle import troute_oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -46,6 +49,8 @@ def test_no_alloc_entry_point_matches_allocating_one_twice():
     assert L.troute_mc_reach_parallel_cfg(*(x.ctypes.data_as(C.c_void_p) for x in (pv, ql, np.int32(rs), np.int32(rl),
                                                                                      qu, qd, dp, qo, vo, dpo)),
                                           10.0, 300.0, nr, None, C.byref(st_ref)) == 0
+    with O.pow_mode(1):
+        oq, ov, od, _ = O.cpu_mc(p, ql, rs, rl, qu, qd, dp, uq=10.0, dt=300.0)
     for _ in range(2):
         o = outs()
         st = T.Stats()
@@ -55,6 +60,8 @@ def test_no_alloc_entry_point_matches_allocating_one_twice():
             rel = np.abs(x - y) / np.maximum(np.abs(y), 1e-300)
             assert rel.max() < 1e-10
         assert st.solves == S and st.iterations == st_ref.iterations
+        for a, b in zip(o, (oq, ov, od)):
+            np.testing.assert_array_equal(a.cpu().numpy(), b)
 
 
 def test_no_alloc_rejects_oversized_calls():
