@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (profiling runs)")
+    ap.add_argument("--no-parity", action="store_true", help="skip the operating-point oracle check")
+    ap.add_argument("--no-batched-plain", action="store_true", help="skip the batched plain-start leg")
     ap.add_argument("--warm", action="store_true",
                     help="learned warm start on a single-network workload (trained on its own plain-run pairs)")
     return ap.parse_args()
@@ -95,6 +97,16 @@ class Dist:
     def barrier(self):
         if self.pg:
             self.pg.barrier()
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
 
     def max(self, x: float) -> float:
         if not self.pg:
@@ -216,20 +228,26 @@ def critical_path_bound(T, w, n_ts: int, it_per_solve: float, sm_mhz, kernel_ms:
     return out
 
 
-def workload(name: str, n_ts: int | None, all_members: bool = True):
+def workload(name: str, n_ts: int | None, members: tuple | None = None):
     """Single networks ('c1', 'c0', 'tree:<segments>', 'c3' = fresh-seed c1
     with warm start) or the batched forms: 'c2' (256 basins with
     LogU(500, 200,000) segments, 288 steps), 'c4' / 'c4w' (64 ensemble
     members of the c1 network, without / with warm start; 32 steps per bench
-    step)."""
+    step). `members` = (first, end): the share of the ensemble members (or of
+    the c2 basins, by index) one rank routes."""
     from troute_gb300 import synth
 
     if name == "c2":
-        nets = synth.basins(seed=1002, n_trees=256)
         T = 288 if n_ts is None else n_ts
+        sizes = synth.basin_sizes(1002, 256)
+        nets = synth.basins(seed=1002, n_trees=256, which=members)
+        qlat = synth.make_qlat(1002, int(sizes.sum()), T)
+        if members is not None:
+            # the same inflow columns as in the unsharded batch
+            offs = np.concatenate([[0], np.cumsum(sizes)])
+            qlat = np.ascontiguousarray(np.concatenate([qlat[:, offs[i]:offs[i + 1]] for i in members], axis=1))
         S = sum(n["topo"]["n_segments"] for n in nets)
-        w = {"name": name, "batch": nets, "n_ts": T, "dt": synth.DT,
-             "qlat": synth.make_qlat(1002, S, T)}
+        w = {"name": name, "batch": nets, "n_ts": T, "dt": synth.DT, "qlat": qlat}
         w["q0"] = np.full(S, synth.Q0)
         w["d0"] = np.full(S, synth.D0)
         w["rl0"] = np.concatenate([np.full(len(n["topo"]["reach_seg_start"]), synth.Q0) for n in nets])
@@ -247,24 +265,38 @@ def workload(name: str, n_ts: int | None, all_members: bool = True):
         w = synth.network(base_net, n_ts=T)
         w["base"] = base_net
         S = w["topo"]["n_segments"]
-        Mg = M if all_members else 1   # the CPU legs route member 0 only
-        qf = np.empty((Mg, S))
-        nf = np.empty((Mg, S))
-        for m in range(Mg):
-            qf[m], nf[m] = synth.make_member(1004, m, S)
-        w.update(name=name, members=M, qfac=qf, nfac=nf, warm=(name == "c4w" or name.endswith(":w")))
-        w["S"], w["R"] = M * S, M * len(w["topo"]["reach_seg_start"])
+        m0, m1 = (0, M) if members is None else members
+        qf = np.empty((m1 - m0, S))
+        nf = np.empty((m1 - m0, S))
+        for k, m in enumerate(range(m0, m1)):
+            qf[k], nf[k] = synth.make_member(1004, m, S)
+        w.update(name=name, members=m1 - m0, member_range=(m0, m1), members_total=M, qfac=qf, nfac=nf,
+                 warm=(name == "c4w" or name.endswith(":w")))
+        w["S"], w["R"] = (m1 - m0) * S, (m1 - m0) * len(w["topo"]["reach_seg_start"])
         w["q0_1"], w["d0_1"], w["rl0_1"] = w["q0"], w["d0"], w["rl0"]
-        w["q0"], w["d0"], w["rl0"] = np.tile(w["q0"], M), np.tile(w["d0"], M), np.tile(w["rl0"], M)
-        return w
-    if name == "c3":
-        w = synth.network("c1", seed=2001, n_ts=n_ts)
-        w["name"], w["warm"] = "c3", True
-        w["S"], w["R"] = w["topo"]["n_segments"], len(w["topo"]["reach_seg_start"])
+        w["q0"], w["d0"], w["rl0"] = (np.tile(w["q0"], m1 - m0), np.tile(w["d0"], m1 - m0),
+                                      np.tile(w["rl0"], m1 - m0))
         return w
     w = synth.network(name, n_ts=n_ts)
+    if name == "c3":
+        w["warm"] = True
     w["S"], w["R"] = w["topo"]["n_segments"], len(w["topo"]["reach_seg_start"])
     return w
+
+
+def shard(name: str, dist) -> tuple | None:
+    """The rank's share of a batched workload (members or basins), or None
+    (single networks run as replicas)."""
+    from troute_gb300 import parallel, synth
+
+    if dist.world <= 1:
+        return None
+    if name in ("c4", "c4w") or name.startswith("ens:"):
+        M = int(name.split(":")[1]) if name.startswith("ens:") else 64
+        return parallel.member_range(M, dist.world, dist.rank)
+    if name == "c2":
+        return tuple(parallel.partition([int(x) for x in synth.basin_sizes(1002, 256)], dist.world)[dist.rank])
+    return None
 
 
 def make_network(T, w, cfg):
@@ -348,19 +380,6 @@ def train_and_plain(T, torch, dev, stream, plain_steps: int, plain_warmup: int, 
     return model, info, plain
 
 
-def single_network(w) -> tuple:
-    """(topo, params, qlat, q0, d0, rl0, label) of the network the CPU legs
-    route: the workload's network, or ensemble member 0 (its perturbed
-    Manning's n and lateral inflow) for the ensembles."""
-    if "members" in w:
-        p = w["params"].copy()
-        p["n_ch"] *= w["nfac"][0]
-        p["ncc"] *= w["nfac"][0]
-        return (w["topo"], p, w["qlat"] * w["qfac"][0][None, :], w["q0_1"], w["d0_1"], w["rl0_1"],
-                "ensemble member 0 of the")
-    return w["topo"], w["params"], w["qlat"], w["q0"], w["d0"], w["rl0"], "the"
-
-
 def topology_bytes_per_seg_step(w) -> float:
     """Reach-topology bytes a step reads per segment, beside the algorithmic
     112 B: per reach its segment range, upstream CSR row and downstream index
@@ -396,69 +415,196 @@ def host_cpu() -> dict:
     return {"nproc": os.cpu_count() or 1, "cpu_model": model or platform.machine()}
 
 
-def cpu_baseline(w) -> dict:
-    """The oracle port of cpu_wavefront_fp64, one core, one routed step of the
-    same network from its initial state (plain secant start, the reference's)."""
+def cpu_baseline(w, win=None) -> dict:
+    """The oracle port of cpu_wavefront_fp64 (the C library's pow(), the
+    reference's arithmetic), one core, one routed step of network 0 of the
+    workload (ensemble member 0, basin 0 or the network) from the start state
+    of the GPU arm's timed window (the initial state without `win`)."""
     from oracle import troute_oracle as O
 
     O.build(ref=False)
     tol = (TIGHT["rtol"], TIGHT["atol"], TIGHT["maxiter"], TIGHT["attempts"])
-    topo, params, qlat, q0, d0, rl0, label = single_network(w)
-    S = topo["n_segments"]
+    ss, rs, cs = member_slice(w, 0)
+    topo, params, qs, label = network_k(w, 0)
+    Sn = topo["n_segments"]
+    ql = w["qlat"][:1, cs] * (qs[None, :] if qs is not None else 1.0)
+    if win is None:
+        q, d, rl, where = w["q0"][ss], w["d0"][ss], w["rl0"][rs], "its initial state"
+    else:
+        q, d, rl, where = win[0][ss], win[1][ss], win[3][rs], "the start state of the timed window"
     t0 = time.perf_counter()
-    O.route_tree(topo, params, qlat[:1], q0, d0, rl0, tol=tol, threads=1)
+    O.route_tree(topo, params, ql, q, d, rl, tol=tol, threads=1)
     dt = time.perf_counter() - t0
-    return {"value": S / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"1 routed step of {label} {S}-segment network from its initial state, rtol 1e-8, "
-                      f"single thread ({dt:.1f} s)", "host": host_cpu()}
+    return {"value": Sn / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"1 routed step of {label} {Sn}-segment network from {where}, rtol 1e-8, single thread "
+                      f"({dt:.1f} s)", "host": host_cpu()}
 
 
 # --------------------------------------------------------------------------- reference arm
+def reference_inputs(name: str, n_ts: int | None):
+    """(network, label, routed steps per bench step) of the reference arm, built
+    with the oracle's own restatement of the seeded generator: this process
+    never loads the product library. The ensembles route member 0."""
+    from oracle import troute_oracle as O
+
+    if name in ("c4", "c4w"):
+        T = 32 if n_ts is None else n_ts
+        w = O.ensemble_member(O.network("c1", n_ts=T), 0)
+        return w, f"member 0 of the 64-member ensemble over the {w['topo']['n_segments']}-segment c1 network", T
+    if name.startswith("ens:"):
+        parts = name.split(":")
+        T = 32 if n_ts is None else n_ts
+        w = O.ensemble_member(O.network(f"tree:{int(parts[2])}", n_ts=T), 0)
+        return w, f"member 0 of the {int(parts[1])}-member ensemble over the tree:{int(parts[2])} network", T
+    if name in ("c0", "c1", "c3") or name.startswith("tree:"):
+        w = O.network(name, n_ts=n_ts)
+        return w, f"the {w['topo']['n_segments']}-segment {name} network", w["n_ts"]
+    return None, "", 0
+
+
 def run_reference(args, dist: Dist):
+    """The reference's CPU algorithm (the oracle port of cpu_wavefront_fp64 in
+    FP64, level-parallel over all host threads; the reference's own routine is
+    single-threaded and is not built on the aarch64 host) on the routed-step
+    window the GPU arm times: the network is first advanced untimed through
+    the GPU arm's warm-up bench steps, then each timed bench step routes the
+    same routed steps as a GPU bench step (lateral inflow rows t mod n_ts, as
+    the GPU arm's graph replays them)."""
     if dist.rank != 0:
         return
     from oracle import troute_oracle as O
 
     O.build(ref=False)
-    w = workload(args.workload, args.n_ts, all_members=False)
-    if "topo" not in w:
+    w, label, per_step = reference_inputs(args.workload, args.n_ts)
+    if w is None:
         print(json.dumps({"impl": "reference", "unavailable": "the CPU arm routes single networks and ensemble "
                                                             "members; run it with --workload c1 for c2"}))
         return
-    topo, params, qlat, q, d, rl, label = single_network(w)
-    S = topo["n_segments"]
+    topo, params, qlat = w["topo"], w["params"], w["qlat"]
+    q, d, rl = w["q0"], w["d0"], w["rl0"]
+    S, R = topo["n_segments"], len(topo["reach_seg_start"])
     nth = os.cpu_count() or 1
     tol = (TIGHT["rtol"], TIGHT["atol"], TIGHT["maxiter"], TIGHT["attempts"])
-    lp, lr = O.levels(topo["reach_up_ptr"], topo["reach_up_idx"], len(topo["reach_seg_start"]))
-    T = qlat.shape[0]
-    times = []
-    for k in range(args.warmup + args.steps):
-        t = k % T
-        t0 = time.perf_counter()
-        o = O.route_tree(topo, params, qlat[t:t + 1], q, d, rl, tol=tol, threads=nth,
-                         level_ptr=lp, level_reach=lr)
-        el = time.perf_counter() - t0
+    lp, lr = O.levels_c(topo["reach_up_ptr"], topo["reach_up_idx"], R)
+    n_ts = qlat.shape[0]
+    per_step = min(per_step, n_ts)
+
+    def route(rows):
+        nonlocal q, d, rl
+        o = O.route_tree(topo, params, rows, q, d, rl, tol=tol, threads=nth, level_ptr=lp, level_reach=lr)
         q, d, rl = o["q"], o["d"], o["reach_last"]
-        if k >= args.warmup:
-            times.append(el)
+        return o["iterations"]
+
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):   # the GPU arm's warm-up bench steps, untimed
+        route(qlat[:per_step])
+    advance_s = time.perf_counter() - t0
+    times, iters = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        iters += route(qlat[:per_step])
+        times.append(time.perf_counter() - t0)
     tot = sum(times)
-    value = S * len(times) / tot
+    value = S * per_step * len(times) / tot
+    first = args.warmup * per_step
+    window = f"routed steps {first}-{first + args.steps * per_step - 1}"
+    sample = (f"{label}: {window} ({args.steps} bench steps of {per_step} routed steps, after {first} untimed "
+              f"routed steps from the initial state in {advance_s:.0f} s), rtol 1e-8, {nth} threads "
+              f"(level-parallel oracle port of cpu_wavefront_fp64; the reference routine is single-threaded)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded generator)",
-            "config": {"workload": f"{args.workload}: FP64 MC secant tree routing of {label} {S}-segment "
-                                   f"network, {len(topo['reach_seg_start'])} reaches, rtol 1e-8, plain secant "
-                                   f"start (the reference's); one routed step per bench step", "segments": S},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
-                             "sample": f"1 routed time step of {label} {S}-segment network per bench step, "
-                                       f"{nth} threads (level-parallel oracle port of cpu_wavefront_fp64)",
+            "data": "synthetic (seeded generator, the oracle's restatement)",
+            "config": {"workload": f"{args.workload}: FP64 MC secant tree routing of {label}, {R} reaches, "
+                                   f"{len(lp) - 1} levels, plain secant start (the reference's), {window}",
+                       "segments": S, "reaches": R, "levels": len(lp) - 1, "routed_steps_per_step": per_step,
+                       "first_timed_routed_step": first, "threads": nth},
+            "solver": {"iterations_per_solve": iters / max(1, S * per_step * len(times))},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port", "sample": sample,
                              "host": host_cpu()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 # --------------------------------------------------------------------------- our arm
+def member_slice(w, k: int = 0):
+    """(segment slice, reach slice, inflow columns) of network k of the handle
+    (an ensemble member or a basin of the batch) in the handle's user order."""
+    if "members" in w:
+        S1, R1 = w["topo"]["n_segments"], len(w["topo"]["reach_seg_start"])
+        return slice(k * S1, (k + 1) * S1), slice(k * R1, (k + 1) * R1), slice(0, S1)
+    if "batch" in w:
+        s0 = sum(n["topo"]["n_segments"] for n in w["batch"][:k])
+        r0 = sum(len(n["topo"]["reach_seg_start"]) for n in w["batch"][:k])
+        n = w["batch"][k]
+        S1, R1 = n["topo"]["n_segments"], len(n["topo"]["reach_seg_start"])
+        return slice(s0, s0 + S1), slice(r0, r0 + R1), slice(s0, s0 + S1)
+    return slice(0, w["S"]), slice(0, w["R"]), slice(0, w["S"])
+
+
+def network_k(w, k: int = 0):
+    """(topo, params, inflow scale or None, label) of network k of the handle."""
+    if "members" in w:
+        p = w["params"].copy()
+        p["n_ch"] *= w["nfac"][k]
+        p["ncc"] *= w["nfac"][k]
+        m = w["member_range"][0] + k
+        return w["topo"], p, w["qfac"][k], f"ensemble member {m} of the"
+    if "batch" in w:
+        n = w["batch"][k]
+        return n["topo"], n["params"], None, f"basin {n['index']} of the batch: the"
+    return w["topo"], w["params"], None, "the"
+
+
+def operating_point_parity(T, w, model, win, after, n_steps: int, qlat_rows) -> dict:
+    """Discharge of network 0 of the handle (ensemble member 0, basin 0 or the
+    network) after the first `n_steps` routed steps of the timed window,
+    routed alone from the window-start state with the start depths recorded,
+    against (a) the same network inside the batched launch (`after`: the
+    handle's state after those steps, or None) and (b) the oracle replaying
+    those solves: correctly rounded powers (bit-identical expected) and the C
+    library's pow() (the reference's arithmetic; ulp-sensitive at rtol 1e-8)."""
+    from oracle import troute_oracle as O
+
+    ss, rs, cs = member_slice(w, 0)
+    topo, params, qs, label = network_k(w, 0)
+    Sn = topo["n_segments"]
+    cfg = T.make_cfg(**TIGHT, warm_start=1 if model else 0, warm_k=WARM_K, record_start=1 if model else 0)
+    if qs is not None:
+        net = T.Network.ensemble(topo, w["params"], 1, n_scale=w["nfac"][0], qlat_scale=qs, cfg=cfg)
+    else:
+        net = T.Network(topo, params, cfg=cfg)
+    if model:
+        net.set_warm_start(model, WARM_DELTA)
+    net.set_state(win[0][ss], win[1][ss], win[3][rs])
+    rows = np.ascontiguousarray(qlat_rows[:n_steps, cs])
+    net.run(rows)
+    q = net.get_state()[0]
+    start = net.start_history(n_steps) if model else None
+    net.close()
+    ql = rows * qs[None, :] if qs is not None else rows
+    tol = (TIGHT["rtol"], TIGHT["atol"], TIGHT["maxiter"], TIGHT["attempts"])
+    nth = os.cpu_count() or 1
+    lp, lr = O.levels_c(topo["reach_up_ptr"], topo["reach_up_idx"], len(topo["reach_seg_start"]))
+    out = {"network": f"{label} {Sn}-segment network", "routed_steps": n_steps,
+           "window": "the first routed steps of the timed window, from the window-start state",
+           "warm_start_replayed": bool(model)}
+    for mode, key in ((1, "max_rel_err"), (0, "max_rel_err_libm_pow")):
+        with O.pow_mode(mode):
+            o = O.route_tree(topo, params, ql, win[0][ss], win[1][ss], win[3][rs], tol=tol, threads=nth,
+                             level_ptr=lp, level_reach=lr, warm_start=start, warm_delta=WARM_DELTA if model else 0.0,
+                             warm_k=WARM_K if model else 0)
+        den = np.maximum(np.abs(o["q"]), 1e-300)
+        out[key] = float(np.max(np.where(q == o["q"], 0.0, np.abs(q - o["q"]) / den)))
+        if mode == 1:
+            out["bit_identical"] = bool(np.array_equal(q, o["q"]))
+    out["oracle_pow"] = {"max_rel_err": "correctly rounded R^(2/3), R^(5/3) (the device's)",
+                         "max_rel_err_libm_pow": "the C library's pow() (the reference's)"}
+    if after is not None:
+        out["alone_vs_batched_bit_identical"] = bool(np.array_equal(q, after[ss]))
+    return out
+
+
 def run_ours(args, dist: Dist):
     import torch
 
@@ -466,11 +612,13 @@ def run_ours(args, dist: Dist):
 
     dev = torch.device("cuda", dist.local if dist.world > 1 else 0)
     torch.cuda.set_device(dev)
-    w = workload(args.workload, args.n_ts)
+    share = shard(args.workload, dist)
+    w = workload(args.workload, args.n_ts, members=share)
     S, R = w["S"], w["R"]
     n_ts = w["qlat"].shape[0]
     cols = w["qlat"].shape[1]
     stream = torch.cuda.Stream(dev)   # a real stream: 0 would mean "the handle's own stream"
+    fp64_rate = T.measure_fp64_rate()  # the FP64 pipe's measured issue rate (roofline peak), untimed
     model = warm_info = plain = None
     if args.warm and "topo" in w and "members" not in w:
         w["warm"] = True
@@ -487,19 +635,26 @@ def run_ours(args, dist: Dist):
     qlat_dev = qlat_host.to(dev, non_blocking=False)
     levels = net.n_levels
     tune = None
+    shape = {}
     if ("batch" in w or "members" in w) and not args.no_tune:
         # the batched forms pick their launch shape with the autotuner (a trial of
-        # half a bench step per candidate, from the same state; untimed)
+        # a quarter bench step per candidate, from the same state; untimed)
         t0 = time.perf_counter()
         trial = max(1, n_ts // 4)
         tune = net.autotune(qlat_dev.data_ptr(), trial, repeats=1, all_mappings=not model)
         tune["tune_s"] = round(time.perf_counter() - t0, 2)
         tune["trial_steps"] = trial
+        shape = dict(mapping=tune["mapping"], blocks_per_sm=tune["blocks_per_sm"],
+                     schedule_flags=tune["schedule_flags"],
+                     threads_per_block=tune["threads_per_block"] if tune["mapping"] == 1 else 0)
     net.graph_capture(qlat_dev.data_ptr(), n_ts)
     for _ in range(args.warmup):
         net.graph_launch(stream.cuda_stream)
     torch.cuda.synchronize(dev)
-    stats_w = net.sync()
+    net.sync()
+    # state at the start of the timed window (host copies): the e2e leg, the
+    # batched plain leg, the parity check and the CPU sample start from it
+    win = net.get_state()
 
     uuid = None
     try:
@@ -528,83 +683,142 @@ def run_ours(args, dist: Dist):
     ms_step = ms_total / args.steps
     kernel_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
     seg_steps = S * n_ts
-    value = seg_steps * args.steps * dist.world / (ms_total / 1e3)
+    total_seg_steps = dist.sum(seg_steps) if share is not None else seg_steps * dist.world
+    value = total_seg_steps * args.steps / (ms_total / 1e3)
 
-    peak, peak_kind = measured_peak_hbm()
+    # roofline: the FP64 pipe (the bound) from this run's own solving warp passes,
+    # against the measured FP64 issue rate; the HBM fraction beside it
+    instr, instr_src = profiled_file("fp64_instr_per_solving_pass", "route_dataflow_instmix_tree200k.md")
+    fp64_warp_instr = stats["solve_passes"] * (instr or 0.0)
+    achieved = fp64_warp_instr * 32 / (kernel_ms / 1e3) / 1e12
+    peak = fp64_rate["warp_instr_per_s"] * 32 / 1e12
+    hbm_peak, peak_kind = measured_peak_hbm()
     alg_bytes = BYTES_PER_SEG_STEP * seg_steps
-    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
+    hbm_achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     tr, tr_src = profiled("dram_bytes_per_seg_step", bool(model))
-    fp64, _ = profiled("fp64_pipe_active_pct", bool(model))
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "alg_bytes_per_seg_step": BYTES_PER_SEG_STEP,
-                "topology_bytes_per_seg_step": topology_bytes_per_seg_step(w),
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": (tr * seg_steps if tr is not None else None),
-                "traffic_source": f"profiles/{tr_src} (DRAM bytes per segment-step x segment-steps of a launch)",
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                "fp64_pipe_active_pct": fp64,
-                "note": "the secant loop is FP64-pipe and dependency bound; DRAM traffic is far below the HBM roofline"}
+                "definition": "FP64 pipe: solving warp passes of the last timed launch (run statistics) x FP64 warp "
+                              "instructions per solving pass x 32 lanes / launch time; peak = the FP64 issue rate "
+                              "measured in this run (troute_measure_fp64_rate, independent DMUL chains on every SM) "
+                              "x 32 lanes; the solver has no FMA contraction, so an FP64 lane operation is a flop",
+                "fp64_instr_per_solving_pass": instr, "instr_source": f"profiles/{instr_src} (ncu instruction mix)",
+                "fp64_peak_warp_instr_per_s": fp64_rate["warp_instr_per_s"],
+                "traffic_source": f"scaled: DRAM bytes per segment-step of the ncu capture in profiles/{tr_src} x "
+                                  f"the segment-steps of one launch (this launch is too large to capture)",
+                "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_achieved / hbm_peak,
+                        "alg_bytes_per_seg_step": BYTES_PER_SEG_STEP,
+                        "topology_bytes_per_seg_step": topology_bytes_per_seg_step(w),
+                        "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                        else "fallback"}}
+
+    # batched plain leg: the same batch and launch shape without the warm start,
+    # from the window-start state (splits the headline into batching and learning)
+    batched_plain = None
+    if model and ("members" in w or "batch" in w) and not args.no_batched_plain:
+        net.set_state(win[0], win[1], win[3])
+        net.set_cfg(T.make_cfg(**TIGHT, **shape))
+        net.graph_capture(qlat_dev.data_ptr(), n_ts)
+        k_plain = min(args.steps, 2)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        for _ in range(k_plain):
+            net.graph_launch(stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        stp = net.sync()
+        bp_ms = dist.max(a.elapsed_time(b))
+        batched_plain = {"value": total_seg_steps * k_plain / (bp_ms / 1e3), "unit": UNIT,
+                         "workload": f"the same batch and launch shape, plain secant start, the first {k_plain} bench "
+                                     f"steps of the timed window from its start state",
+                         "iterations_per_solve": stp["iterations"] / max(1, stp["solves"]),
+                         "ms_per_step": bp_ms / k_plain}
+    net.close()
 
     e2e = None
+    after = None
     if not args.no_e2e:
         # public C-ABI path with host buffers: H2D of the step's lateral inflow
-        # from pinned memory inside troute_run, D2H of the routed state
+        # from pinned memory inside troute_run, D2H of the routed state into
+        # pinned buffers; the same routed steps as the timed window's first bench
+        # steps (from the window-start state)
         qh = qlat_host.numpy()
-        net.close()
         net2 = make_network(T, w, cfg)
         if model:
             net2.set_warm_start(model, WARM_DELTA)
-        net2.set_state(w["q0"], w["d0"], w["rl0"])
-        if tune:
-            net2.set_cfg(T.make_cfg(**TIGHT, warm_start=1 if model else 0, warm_k=WARM_K, mapping=tune["mapping"],
-                                    blocks_per_sm=tune["blocks_per_sm"], schedule_flags=tune["schedule_flags"],
-                                    threads_per_block=tune["threads_per_block"] if tune["mapping"] == 1 else 0))
-        e2e_steps = min(args.steps, 2) if "members" in w else args.steps
-        for _ in range(1):
-            net2.run(qh)
-            net2.get_state()
+        if shape:
+            net2.set_cfg(T.make_cfg(**TIGHT, warm_start=1 if model else 0, warm_k=WARM_K, **shape))
+        # two sets of pinned state buffers, used in turn: the first bench step's
+        # discharge stays readable for the parity check without a copy in the loop
+        outs = []
+        for _ in range(2):
+            o = [torch.empty(S, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+            outs.append(o + [torch.empty(R, dtype=torch.float64, pin_memory=True).numpy()])
+        e2e_steps = min(args.steps, 2) if ("members" in w or "batch" in w) else args.steps
+        net2.set_state(win[0], win[1], win[3])
         torch.cuda.synchronize(dev)
         dist.barrier()
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
+        for k in range(e2e_steps):
             net2.run(qh)
-            net2.get_state()
+            net2.get_state(out=outs[k % 2])
         t1 = time.perf_counter()
+        after = outs[0][0]
         dist.barrier()
         e2e_s = dist.max(t1 - t0)
-        e2e = {"value": seg_steps * e2e_steps * dist.world / e2e_s, "unit": UNIT,
+        e2e = {"value": total_seg_steps * e2e_steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(qh.nbytes), "d2h_bytes_per_step": int((3 * S + R) * 8),
-               "steps": e2e_steps}
+               "steps": e2e_steps, "window": "the first bench steps of the timed window, from its start state"}
         net2.close()
 
-    cpu = None
-    if dist.rank == 0 and not args.no_cpu_baseline and "topo" in w:
-        cpu = cpu_baseline(w)
+    parity = cpu = None
+    if dist.rank == 0 and not args.no_parity:
+        n_par = min(n_ts, 32)
+        parity = operating_point_parity(T, w, model, win, after if n_par == n_ts else None, n_par, w["qlat"])
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, win)
     it = stats["iterations"]
     crit = critical_path_bound(T, w, n_ts, it / max(1, stats["solves"]), clocks.get("sm_mhz"), kernel_ms)
+    if share is not None:
+        par = (f"{dist.world} ranks, batch sharded without exchange: rank 0 routes "
+               + (f"members {share[0]}-{share[1] - 1}" if "members" in w else f"{len(share)} basins"))
+        scaling = "strong"
+    else:
+        par = "replicas" if dist.world > 1 else "single GPU"
+        scaling = "weak"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": scaling,
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
             "config": {"workload": f"{args.workload}: FP64 MC secant tree routing ({describe(w)}), "
                                    f"{S} segments, {R} reaches, {levels} levels, {n_ts} steps of "
-                                   f"{w['dt']:.0f} s per bench step, rtol 1e-8 atol 1e-10",
+                                   f"{w['dt']:.0f} s per bench step, rtol 1e-8 atol 1e-10; timed window: routed "
+                                   f"steps {args.warmup * n_ts}-{(args.warmup + args.steps) * n_ts - 1}",
                        "segments": S, "reaches": R, "levels": levels, "timesteps_per_step": n_ts,
+                       "first_timed_routed_step": args.warmup * n_ts,
                        "l2": f"inputs larger than L2 (129 MB): lateral inflow {w['qlat'].nbytes / 1e9:.2f} GB and "
                              f"segment parameters {S * 96 / 1e9:.2f} GB read per bench step",
-                       "parallelism": "replicas" if dist.world > 1 else "single GPU"},
+                       "parallelism": par},
             "roofline": roofline, "critical_path": crit, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": 4 * args.steps,
+            "gpu_launches": 4 * args.steps, "parity": parity,
+            "max_rel_err": None if parity is None else parity["max_rel_err"],
             "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
                        "early_exits": stats["early_exits"], "warm_used": stats["warm_used"],
                        "warm_fallback_rate": stats["warm_fallback"] / max(1, stats["warm_used"]),
                        "busy_lanes_per_warp_pass": stats["lane_busy"] / max(1, stats["warp_passes"]),
                        "busy_lanes_per_solving_pass": stats["lane_busy"] / max(1, stats["solve_passes"]),
-                       "solving_passes_share": stats["solve_passes"] / max(1, stats["warp_passes"])}}
+                       "solving_passes_share": stats["solve_passes"] / max(1, stats["warp_passes"]),
+                       "solving_warp_passes": stats["solve_passes"]}}
     if tune:
         line["autotune"] = tune
     if model:
         line["warm_model"] = warm_info
         line["plain_single_basin"] = plain
         line["speedup_vs_plain"] = value / plain["value"]
+        if batched_plain:
+            line["batched_plain"] = batched_plain
+            line["speedup_split"] = {"batching": batched_plain["value"] / plain["value"],
+                                     "learned_warm_start": value / batched_plain["value"]}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 

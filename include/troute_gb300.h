@@ -315,6 +315,13 @@ int troute_get_start_history(troute_handle* h, double* start_hist, int n_ts);
  * stays usable. Exercises the device failure path without faulting. */
 int troute_debug_timeout_probe(long long wait_cycles);
 
+/* Measures the current device's FP64 issue rate: independent DMUL chains on
+ * every SM (32 warps per SM), launches of >= 20 ms, best of several; returns
+ * FP64 warp instructions per second (and the launch time). The routing
+ * kernels are bound by this pipe; the benchmark sets their FP64 instruction
+ * rate against it. No counterpart in the reference. */
+int troute_measure_fp64_rate(double* warp_instr_per_s, double* ms);
+
 /* Evaluates, on the device, the solver's pow(x, 2/3) and pow(x, 5/3) for n
  * host values: out = [ours_23[n], ours_53[n], cuda_pow_23[n], cuda_pow_53[n]]
  * (the last two from CUDA's pow(), for accuracy checks). */

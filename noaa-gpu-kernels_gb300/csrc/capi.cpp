@@ -234,6 +234,48 @@ extern "C" int troute_debug_timeout_probe(long long wait_cycles)
     return set_error(TROUTE_ESTATE, "probe did not report a timeout");
 }
 
+extern "C" int troute_measure_fp64_rate(double* warp_instr_per_s, double* ms)
+{
+    if (!warp_instr_per_s) return set_error(TROUTE_EINVAL, "null output");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_error(TROUTE_ENODEV, "no CUDA device");
+    int dev = 0, sms = 0;
+    int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (!rc) rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+    if (rc) return rc;
+    const int blocks = 4 * sms;   // 32 warps per SM
+    DevPtr sink;
+    if ((rc = cuda_check(cudaMalloc(&sink.p, (size_t)blocks * sizeof(double)), "cudaMalloc"))) return rc;
+    cudaEvent_t e0, e1;
+    if ((rc = cuda_check(cudaEventCreate(&e0), "event"))) return rc;
+    if ((rc = cuda_check(cudaEventCreate(&e1), "event"))) { cudaEventDestroy(e0); return rc; }
+    double best = 0.0, best_ms = 0.0, wi = 0.0;
+    int iters = 2048;
+    for (int rep = 0; rep < 6 && !rc; ++rep) {
+        cudaEventRecord(e0, nullptr);
+        rc = launch_fp64_rate(blocks, iters, static_cast<double*>(sink.p), nullptr, &wi);
+        cudaEventRecord(e1, nullptr);
+        if (!rc) rc = cuda_check(cudaEventSynchronize(e1), "fp64 rate");
+        float t = 0.f;
+        if (!rc) cudaEventElapsedTime(&t, e0, e1);
+        if (!rc && t > 0.f) {
+            if (t < 20.f && iters < (1 << 24)) {   // grow to a launch of >= 20 ms, then keep the best
+                iters *= 2;
+                --rep;
+                continue;
+            }
+            const double r = wi / (t * 1e-3);
+            if (r > best) { best = r; best_ms = t; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    *warp_instr_per_s = best;
+    if (ms) *ms = best_ms;
+    return TROUTE_OK;
+}
+
 extern "C" int troute_debug_pow(const double* x, int n, double* out)
 {
     if (n < 0 || (n > 0 && (!x || !out))) return set_error(TROUTE_EINVAL, "bad arguments");

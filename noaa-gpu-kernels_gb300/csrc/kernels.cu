@@ -352,6 +352,35 @@ int launch_debug_pow(const double* x, int n, double* out, void* stream)
     return cuda_status(cudaGetLastError(), "debug pow launch");
 }
 
+// FP64 issue-rate probe: every thread runs kFp64Chains independent chains of
+// multiplications by a and 1/a in turn (the values stay near their start, no
+// overflow, no denormals); each chain step is one DMUL warp instruction per
+// warp. The sum is stored so nothing is optimised away.
+constexpr int kFp64Chains = 8;
+__global__ void __launch_bounds__(256) fp64_rate_kernel(double a, double ainv, int iters, double* sink)
+{
+    double x[kFp64Chains];
+#pragma unroll
+    for (int c = 0; c < kFp64Chains; ++c) x[c] = 1.0 + 1e-3 * (double)(threadIdx.x * kFp64Chains + c);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < kFp64Chains; ++c) x[c] = x[c] * a;
+#pragma unroll
+        for (int c = 0; c < kFp64Chains; ++c) x[c] = x[c] * ainv;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kFp64Chains; ++c) s += x[c];
+    if (s == 12345.678) sink[blockIdx.x] = s;   // never true; keeps the chains live
+}
+
+int launch_fp64_rate(int blocks, int iters, double* sink, void* stream, double* warp_instr)
+{
+    fp64_rate_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(1.0000001, 1.0 / 1.0000001, iters, sink);
+    *warp_instr = (double)blocks * (256 / 32) * (double)iters * 2.0 * kFp64Chains;
+    return cuda_status(cudaGetLastError(), "fp64 rate launch");
+}
+
 int launch_timeout_probe(DevStats* stats, long long wait_cycles, void* stream)
 {
     timeout_probe_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(stats, wait_cycles);

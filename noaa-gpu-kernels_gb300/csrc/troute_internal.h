@@ -165,6 +165,7 @@ int launch_scatter(const double* src, const long long* map, long long n, double*
 int launch_gather(const double* src, const long long* map, long long n, double* dst,
                   void* stream);
 int launch_timeout_probe(DevStats* stats, long long wait_cycles, void* stream);
+int launch_fp64_rate(int blocks, int iters, double* sink, void* stream, double* warp_instr);
 int launch_debug_pow(const double* x, int n, double* out, void* stream);
 int launch_debug_div(const double* a, const double* b, int n, double* out, void* stream);
 int launch_debug_quot_gt(const double* a, const double* b, double c, int n, int* out, void* stream);

@@ -172,6 +172,7 @@ _SIGS = {
     "troute_write_network": ([C.c_char_p, _P], _I),
     "troute_debug_timeout_probe": ([C.c_longlong], _I),
     "troute_debug_pow": ([_P, _I, _P], _I),
+    "troute_measure_fp64_rate": ([_P, _P], _I),
     "troute_debug_div": ([_P, _P, _I, _P], _I),
     "troute_debug_quot_gt": ([_P, _P, C.c_double, _I, _P], _I),
     "troute_levels": ([_I, _P, _P, _P, _P, _P, _P], _I),
@@ -252,6 +253,14 @@ def make_cfg(rtol=0.01, atol=0.01, maxiter=100, attempts=5, **kw) -> Cfg:
 def timeout_probe(wait_cycles: int = 2_000_000) -> int:
     """Runs the bounded-wait probe kernel; returns the status code (ETIMEOUT expected)."""
     return lib().troute_debug_timeout_probe(int(wait_cycles))
+
+
+def measure_fp64_rate() -> dict:
+    """The device's FP64 issue rate (independent DMUL chains on every SM):
+    FP64 warp instructions per second and the probe launch's time."""
+    r, ms = C.c_double(), C.c_double()
+    _check(lib().troute_measure_fp64_rate(C.byref(r), C.byref(ms)))
+    return {"warp_instr_per_s": r.value, "ms": ms.value}
 
 
 def debug_pow(x):
@@ -465,9 +474,16 @@ class Network:
         r = None if reach_last is None else _f64(reach_last, self.n_reaches)
         _check(lib().troute_set_state(self._h, _ptr(q), _ptr(d), _ptr(r)))
 
-    def get_state(self):
-        q, d, v, r = (np.zeros(self.n_segments), np.zeros(self.n_segments), np.zeros(self.n_segments),
-                      np.zeros(self.n_reaches))
+    def get_state(self, out=None):
+        """(discharge, depth, velocity, reach outflow) in user order; `out`: four
+        caller arrays (e.g. pinned host memory) to fill instead of new ones."""
+        if out is None:
+            out = (np.zeros(self.n_segments), np.zeros(self.n_segments), np.zeros(self.n_segments),
+                   np.zeros(self.n_reaches))
+        q, d, v, r = out
+        for a, n in ((q, self.n_segments), (d, self.n_segments), (v, self.n_segments), (r, self.n_reaches)):
+            if a.dtype != np.float64 or a.size != n or not a.flags["C_CONTIGUOUS"] or not a.flags["WRITEABLE"]:
+                raise ValueError("get_state: out arrays must be contiguous writable float64 of the state's sizes")
         _check(lib().troute_get_state(self._h, _ptr(q), _ptr(d), _ptr(v), _ptr(r)))
         return q, d, v, r
 

@@ -14,8 +14,10 @@ from concurrent.futures import ThreadPoolExecutor
 
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG_ROOT, "csrc")
-BUILD = os.path.join(PKG_ROOT, "_build")
-LIBDIR = os.path.join(PKG_ROOT, "lib")
+# TROUTE_BUILD_DIR / TROUTE_LIB_DIR place a variant build (e.g. the
+# self-checking one, TROUTE_CHECK=1) beside the default one
+BUILD = os.environ.get("TROUTE_BUILD_DIR") or os.path.join(PKG_ROOT, "_build")
+LIBDIR = os.environ.get("TROUTE_LIB_DIR") or os.path.join(PKG_ROOT, "lib")
 LIB = os.path.join(LIBDIR, "libtroute_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 

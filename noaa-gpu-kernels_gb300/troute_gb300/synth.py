@@ -4,7 +4,11 @@ library's platform-independent generator).
   c0  random binary merge tree, 1,000 segments in ~200 reaches of 1-10
       segments, 288 steps (CPU-runnable parity case)
   c1  2.7M segments in ~1.1M reaches (uniform random binary tree with 550,000
-      headwaters: Horton bifurcation ratio ~4, ~3,000 levels), 144 steps
+      headwaters: Horton bifurcation ratio ~4), 144 steps. The depth of such
+      a tree varies with the seed (1,666 to 4,287 levels over seeds
+      1001-1030); seed 1010 gives 3,016 levels, the specified ~3,000
+  c3  c1's sizes on a fresh seed (2006: 2,912 levels), for the warm start
+      trained on c1
   c2  256 independent trees with LogU(500, 200,000) segments, 288 steps
   c4  64 ensemble members of the c1 network: lateral inflow x LogN(0, 0.3),
       Manning's n x U(0.8, 1.2), 288 steps
@@ -24,6 +28,8 @@ DT = 300.0
 Q0 = 0.1
 D0 = 0.1
 SEG_PER_REACH = 2.7e6 / 1.1e6
+C1_SEED = 1010   # 3,016 levels
+C3_SEED = 2006   # 2,912 levels
 
 
 def make_tree(seed: int, n_leaves: int, n_segments: int, max_len: int = 10) -> dict:
@@ -71,13 +77,13 @@ def tree_size(n_segments: int) -> int:
 
 
 def network(name: str, seed: int | None = None, n_ts: int | None = None, with_qlat: bool = True) -> dict:
-    """One of the single-network workloads ('c0', 'c1', or 'tiny' for tests)."""
+    """One of the single-network workloads ('c0', 'c1', 'c3' or 'tree:<segments>')."""
     if name == "c0":
         seed = 1000 if seed is None else seed
         topo = make_tree(seed, 100, 1000, 10)
         T = 288 if n_ts is None else n_ts
-    elif name == "c1":
-        seed = 1001 if seed is None else seed
+    elif name in ("c1", "c3"):
+        seed = (C1_SEED if name == "c1" else C3_SEED) if seed is None else seed
         topo = make_tree(seed, 550_000, 2_700_000, 10)
         T = 144 if n_ts is None else n_ts
     elif name.startswith("tree:"):
@@ -96,14 +102,23 @@ def network(name: str, seed: int | None = None, n_ts: int | None = None, with_ql
     return out
 
 
-def basins(seed: int = 1002, n_trees: int = 256, lo: float = 500.0, hi: float = 200_000.0, scale: float = 1.0):
-    """c2: independent trees with LogU(lo, hi) segments each (times `scale`)."""
+def basin_sizes(seed: int = 1002, n_trees: int = 256, lo: float = 500.0, hi: float = 200_000.0,
+                scale: float = 1.0) -> np.ndarray:
+    """c2's segment counts: LogU(lo, hi) per tree (times `scale`), at least 3."""
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_trees)) * scale
-    sizes = np.maximum(3, np.round(sizes)).astype(int)
+    return np.maximum(3, np.round(sizes)).astype(int)
+
+
+def basins(seed: int = 1002, n_trees: int = 256, lo: float = 500.0, hi: float = 200_000.0, scale: float = 1.0,
+           which=None):
+    """c2: independent trees with LogU(lo, hi) segments each (times `scale`);
+    `which` selects basins by index (a rank's share), default all."""
+    sizes = basin_sizes(seed, n_trees, lo, hi, scale)
     nets = []
-    for i, S in enumerate(sizes):
+    for i in (range(n_trees) if which is None else which):
+        S = int(sizes[i])
         s = seed * 1000 + i
-        topo = make_tree(s, tree_size(int(S)), int(S), 10)
-        nets.append({"topo": topo, "params": make_params(s, int(S)), "seed": s})
+        topo = make_tree(s, tree_size(S), S, 10)
+        nets.append({"topo": topo, "params": make_params(s, S), "seed": s, "index": int(i)})
     return nets

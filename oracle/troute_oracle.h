@@ -16,6 +16,8 @@
 #ifndef TROUTE_ORACLE_H
 #define TROUTE_ORACLE_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -151,6 +153,19 @@ typedef struct oracle_diff_reach {
 } oracle_diff_reach;
 int oracle_diffusive_tridiag(const oracle_diff_reach* rp, const float* dx, const float* diffusivity,
                              const float* qp_prev, float* qp_out, int n_reaches, int max_nodes);
+
+/* Seeded synthetic inputs (oracle_gen.c), byte for byte the product
+ * generator's: tree topology (returns 0, or 1 for bad sizes, 2 out of memory),
+ * channel parameters, lateral inflow [n_ts][n_segments] for steps t0..,
+ * ensemble member factors (either may be NULL). */
+int oracle_gen_tree(uint64_t seed, int n_leaves, int n_segments, int max_len, int* seg_start, int* seg_len,
+                    int* up_ptr, int* up_idx);
+void oracle_gen_params(uint64_t seed, int n_segments, oracle_chparams* p);
+int oracle_gen_qlat(uint64_t seed, int n_segments, int t0, int n_ts, double dt, double* qlat, int n_threads);
+void oracle_gen_member(uint64_t seed, int member, int n_segments, double* qfac, double* nfac);
+/* Level schedule by the reference's rule (gen_network.py:219-231); returns the
+ * number of levels (level_ptr has n_reaches + 1 entries of room). */
+int oracle_levels(int n_reaches, const int* up_ptr, const int* up_idx, int* level_ptr, int* level_reach);
 
 #ifdef __cplusplus
 }

@@ -82,6 +82,16 @@ def oracle():
         L.oracle_set_pow_mode.restype = None
         L.oracle_pow23_53.argtypes = [C.c_double, _P, _P]
         L.oracle_pow23_53.restype = None
+        L.oracle_gen_tree.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int] + [_P] * 4
+        L.oracle_gen_tree.restype = C.c_int
+        L.oracle_gen_params.argtypes = [C.c_uint64, C.c_int, _P]
+        L.oracle_gen_params.restype = None
+        L.oracle_gen_qlat.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_double, _P, C.c_int]
+        L.oracle_gen_qlat.restype = C.c_int
+        L.oracle_gen_member.argtypes = [C.c_uint64, C.c_int, C.c_int, _P, _P]
+        L.oracle_gen_member.restype = None
+        L.oracle_levels.argtypes = [C.c_int, _P, _P, _P, _P]
+        L.oracle_levels.restype = C.c_int
         _ORC = L
     return _ORC
 
@@ -366,4 +376,100 @@ def diffusive_tridiag(reaches, dx, diffusivity, qp_prev, qp_out=None, use_ref=Fa
         rc = oracle().oracle_diffusive_tridiag(_ptr(rp), _ptr(dx), _ptr(df), _ptr(qp), _ptr(out), n, m)
         if rc:
             raise RuntimeError(f"oracle_diffusive_tridiag failed: {rc}")
+    return out
+
+
+# --------------------------------------------------------------------------- seeded inputs
+# The benchmark's synthetic workloads, built by the oracle's own restatement of
+# the product's seeded generator (oracle_gen.c), so that the CPU legs never load
+# the product library. tests/test_generator.py checks every array against the
+# product generator byte for byte.
+DT, Q0, D0 = 300.0, 0.1, 0.1
+SEG_PER_REACH = 2.7e6 / 1.1e6
+C1_SEED, C3_SEED, C0_SEED, TREE_SEED, MEMBER_SEED = 1010, 2006, 1000, 7, 1004
+
+
+def gen_tree(seed: int, n_leaves: int, n_segments: int, max_len: int = 10) -> dict:
+    R = 2 * n_leaves - 1
+    seg_start, seg_len = np.zeros(R, np.int32), np.zeros(R, np.int32)
+    up_ptr, up_idx = np.zeros(R + 1, np.int32), np.zeros(max(R - 1, 1), np.int32)
+    rc = oracle().oracle_gen_tree(seed, n_leaves, n_segments, max_len, _ptr(seg_start), _ptr(seg_len), _ptr(up_ptr),
+                                  _ptr(up_idx))
+    if rc:
+        raise ValueError(f"oracle_gen_tree: {rc}")
+    return {"n_segments": int(n_segments), "reach_seg_start": seg_start, "reach_seg_len": seg_len,
+            "reach_up_ptr": up_ptr, "reach_up_idx": up_idx[: R - 1]}
+
+
+def gen_params(seed: int, n_segments: int) -> np.ndarray:
+    p = np.zeros(n_segments, CHP)
+    oracle().oracle_gen_params(seed, n_segments, _ptr(p))
+    return p
+
+
+def gen_qlat(seed: int, n_segments: int, n_ts: int, t0: int = 0, dt: float = DT, threads: int = 0) -> np.ndarray:
+    q = np.zeros((n_ts, n_segments))
+    rc = oracle().oracle_gen_qlat(seed, n_segments, t0, n_ts, dt, _ptr(q), int(threads or os.cpu_count() or 1))
+    if rc:
+        raise MemoryError("oracle_gen_qlat")
+    return q
+
+
+def gen_member(seed: int, member: int, n_segments: int):
+    qf, nf = np.zeros(n_segments), np.zeros(n_segments)
+    oracle().oracle_gen_member(seed, member, n_segments, _ptr(qf), _ptr(nf))
+    return qf, nf
+
+
+def levels_c(up_ptr, up_idx, R: int):
+    """levels() computed in C (the same schedule, for networks of millions of reaches)."""
+    up_ptr = np.ascontiguousarray(up_ptr, np.int32)
+    up_idx = np.ascontiguousarray(up_idx if len(up_idx) else [0], np.int32)
+    lp, lr = np.zeros(R + 1, np.int32), np.zeros(max(R, 1), np.int32)
+    L = oracle().oracle_levels(R, _ptr(up_ptr), _ptr(up_idx), _ptr(lp), _ptr(lr))
+    if L < 0:
+        raise MemoryError("oracle_levels")
+    return lp[: L + 1], lr[:R]
+
+
+def tree_size(n_segments: int) -> int:
+    """Headwaters of a tree with ~2.45 segments per reach."""
+    n_leaves = max(1, int(round(n_segments / SEG_PER_REACH / 2.0)))
+    return min(n_leaves, (n_segments + 1) // 2)
+
+
+def network(name: str, seed: int | None = None, n_ts: int | None = None, t0: int = 0) -> dict:
+    """The single-network workloads: 'c0' (1,000 segments, 288 steps), 'c1'
+    (2.7M segments, ~3,000 levels, 144 steps), 'c3' (c1's sizes on a fresh
+    seed) and 'tree:<segments>' (24 steps); lateral inflow of steps t0.."""
+    if name == "c0":
+        seed = C0_SEED if seed is None else seed
+        topo, T = gen_tree(seed, 100, 1000, 10), 288
+    elif name in ("c1", "c3"):
+        seed = (C1_SEED if name == "c1" else C3_SEED) if seed is None else seed
+        topo, T = gen_tree(seed, 550_000, 2_700_000, 10), 144
+    elif name.startswith("tree:"):
+        S = int(name.split(":")[1])
+        seed = TREE_SEED if seed is None else seed
+        topo, T = gen_tree(seed, tree_size(S), S, 10), 24
+    else:
+        raise ValueError(name)
+    T = T if n_ts is None else n_ts
+    S = topo["n_segments"]
+    R = len(topo["reach_seg_start"])
+    return {"name": name, "seed": seed, "topo": topo, "params": gen_params(seed, S), "n_ts": T, "dt": DT,
+            "qlat": gen_qlat(seed, S, T, t0), "q0": np.full(S, Q0), "d0": np.full(S, D0), "rl0": np.full(R, Q0)}
+
+
+def ensemble_member(w: dict, member: int, seed: int = MEMBER_SEED) -> dict:
+    """Member `member` of an ensemble over network w: Manning's n (channel and
+    floodplain) times U(0.8, 1.2) and lateral inflow times LogN(0, 0.3), per
+    segment, the products formed in FP64 as the library forms them."""
+    S = w["topo"]["n_segments"]
+    qf, nf = gen_member(seed, member, S)
+    p = w["params"].copy()
+    p["n_ch"] *= nf
+    p["ncc"] *= nf
+    out = dict(w)
+    out.update(params=p, qlat=w["qlat"] * qf[None, :], qfac=qf, nfac=nf, member=member)
     return out

@@ -14,11 +14,12 @@ maximum relative error on discharge reported for every config:
   depends on the starting bracket), so one misrounded power can move a
   converged depth by far more than an ulp.
 
-Configs: c1 (2.7 M segments, 2 steps), c2 (256 basins, 12.0 M segments,
-1 step), c4 (64 members of c1, 1 step, members 0 and 63 checked), c4w (c4
-with the learned warm start), c3 (a fresh-seed c1 network routed with the
-model trained on c1), from the initial state. Each line printed is
-`PARITY <config> <tolerance> <oracle> max_rel=<value>`.
+Configs: c1 (2.7 M segments, 2 steps, and the whole 144-step run), c2 (256
+basins, 8.3 M segments, 1 step), c4 (64 members of c1, 1 step, members 0 and
+63 checked), c4w (c4 with the learned warm start: 1 step from the initial
+state, and the benchmark's timed window, routed steps 96-127), c3 (a
+fresh-seed c1 network routed with the model trained on c1). Each line printed
+is `PARITY <config> <tolerance> <oracle> max_rel=<value>`.
 """
 import os
 
@@ -182,7 +183,7 @@ def test_c4w_warm_start_replays(c1, members, model):
 
 
 def test_c3_fresh_network_warm_start_replays(model):
-    w = synth.network("c1", seed=2001, n_ts=1)
+    w = synth.network("c3", n_ts=1)
     cfg = cfg_of(TIGHT, warm_start=1, warm_k=16, record_start=1)
     with T.Network(w["topo"], w["params"], cfg=cfg) as net:
         net.set_warm_start(model, 0.05)
@@ -193,3 +194,63 @@ def test_c3_fresh_network_warm_start_replays(model):
     o = oracle(w, w["params"], w["qlat"], TIGHT, 1, warm_start=start, warm_delta=0.05, warm_k=16)
     report("c3", TIGHT, "crpow warm replay", max_rel(q, o["q"]))
     np.testing.assert_array_equal(q, o["q"])
+
+
+def test_c1_whole_144_step_run():
+    """The c1 benchmark run in full (144 steps from the initial state, rtol
+    1e-8): bit-identical to the oracle with correctly rounded powers -- final
+    discharge, depth and the total iteration count; the C-library-pow
+    oracle's distance is printed."""
+    w = synth.network("c1")
+    assert w["qlat"].shape[0] == 144
+    args = (w["topo"], w["params"], w["qlat"], w["q0"], w["d0"], w["rl0"])
+    g = T.route_tree(*args, cfg=cfg_of(TIGHT))
+    o1 = oracle(w, w["params"], w["qlat"], TIGHT, 1)
+    report("c1 144 steps", TIGHT, "crpow", max_rel(g["q"], o1["q"]))
+    np.testing.assert_array_equal(g["q"], o1["q"])
+    np.testing.assert_array_equal(g["d"], o1["d"])
+    assert g["stats"]["iterations"] == o1["iterations"]
+    report("c1 144 steps", TIGHT, "libm", max_rel(g["q"], oracle(w, w["params"], w["qlat"], TIGHT, 0)["q"]))
+
+
+def test_c4w_at_the_benchmark_operating_point(members, model):
+    """The benchmark's timed window: the 64-member warm-started ensemble is
+    routed from the initial state through three 32-step launches (routed steps
+    0-95, the bench's warm-up), then one more 32-step launch (steps 96-127).
+    Members 0 and 63, routed alone from the step-96 state with their starting
+    depths recorded, equal their results inside the batched launch bit for bit,
+    and the oracle replaying those solves (correctly rounded powers) equals
+    both; the C-library-pow distance is printed."""
+    qf, nf = members
+    w = synth.network("c1", n_ts=32)
+    S = w["topo"]["n_segments"]
+    R = len(w["topo"]["reach_seg_start"])
+    M = 64
+    cfg = cfg_of(TIGHT, warm_start=1, warm_k=16)
+    with T.Network.ensemble(w["topo"], w["params"], M, n_scale=nf, qlat_scale=qf, cfg=cfg) as net:
+        net.set_warm_start(model, 0.05)
+        net.set_state(np.tile(w["q0"], M), np.tile(w["d0"], M), np.tile(w["rl0"], M))
+        for _ in range(3):
+            net.run(w["qlat"])
+        q96, d96, _, rl96 = net.get_state()
+        st = net.run(w["qlat"])
+        q128 = net.get_state()[0]
+    assert st["warm_used"] > 0.9 * (st["solves"] - st["early_exits"])
+    cfg_rec = cfg_of(TIGHT, warm_start=1, warm_k=16, record_start=1)
+    for m in MEMBERS:
+        ss, rs = slice(m * S, (m + 1) * S), slice(m * R, (m + 1) * R)
+        with T.Network.ensemble(w["topo"], w["params"], 1, n_scale=nf[m], qlat_scale=qf[m], cfg=cfg_rec) as one:
+            one.set_warm_start(model, 0.05)
+            one.set_state(q96[ss], d96[ss], rl96[rs])
+            one.run(w["qlat"])
+            q_alone = one.get_state()[0]
+            start = one.start_history(32)
+        np.testing.assert_array_equal(q_alone, q128[ss])
+        net_m = dict(w, q0=q96[ss], d0=d96[ss], rl0=rl96[rs])
+        p = member_params(w, nf, m)
+        ql = w["qlat"] * qf[m][None, :]
+        o = oracle(net_m, p, ql, TIGHT, 1, warm_start=start, warm_delta=0.05, warm_k=16)
+        report(f"c4w member {m} steps 96-127", TIGHT, "crpow warm replay", max_rel(q128[ss], o["q"]))
+        np.testing.assert_array_equal(q128[ss], o["q"])
+        o0 = oracle(net_m, p, ql, TIGHT, 0, warm_start=start, warm_delta=0.05, warm_k=16)
+        report(f"c4w member {m} steps 96-127", TIGHT, "libm warm replay", max_rel(q128[ss], o0["q"]))

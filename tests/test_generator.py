@@ -63,3 +63,53 @@ def test_member_factors():
     qf, nf = synth.make_member(9, 3, 20000)
     assert abs(np.log(qf).std() - 0.3) < 0.01 and abs(np.log(qf).mean()) < 0.01
     assert 0.8 <= nf.min() and nf.max() <= 1.2
+
+
+def test_oracle_generator_is_byte_identical():
+    """The CPU legs build their inputs with the oracle's restatement of the
+    generator (they must not load the product library): every array equals
+    the product's, byte for byte, including a multi-threaded inflow matrix."""
+    from oracle import troute_oracle as O
+
+    for seed, leaves, segs in ((1000, 100, 1000), (7, 4081, 20000), (1010, 20000, 49000)):
+        a, b = synth.make_tree(seed, leaves, segs), O.gen_tree(seed, leaves, segs)
+        for k in ("reach_seg_start", "reach_seg_len", "reach_up_ptr", "reach_up_idx"):
+            assert a[k].tobytes() == b[k].tobytes(), (seed, k)
+        assert synth.make_params(seed, segs).tobytes() == O.gen_params(seed, segs).tobytes()
+    for t0 in (0, 96):
+        assert synth.make_qlat(11, 30000, 40, t0=t0).tobytes() == O.gen_qlat(11, 30000, 40, t0=t0, threads=4).tobytes()
+    for m in (0, 63):
+        qa, na = synth.make_member(1004, m, 30000)
+        qb, nb = O.gen_member(1004, m, 30000)
+        assert qa.tobytes() == qb.tobytes() and na.tobytes() == nb.tobytes()
+    for name in ("c0", "tree:20000"):
+        a, b = synth.network(name, n_ts=4), O.network(name, n_ts=4)
+        assert a["seed"] == b["seed"] and a["params"].tobytes() == b["params"].tobytes()
+        assert a["qlat"].tobytes() == b["qlat"].tobytes()
+    # the named seeds agree (c1 and c3 themselves are checked on their topology)
+    assert (O.C1_SEED, O.C3_SEED) == (synth.C1_SEED, synth.C3_SEED)
+
+
+def test_oracle_levels_in_c_match_the_reference_rule():
+    from oracle import troute_oracle as O
+
+    t = synth.make_tree(5, 3000, 7400)
+    R = len(t["reach_seg_start"])
+    lp, lr = O.levels(t["reach_up_ptr"], t["reach_up_idx"], R)
+    lp2, lr2 = O.levels_c(t["reach_up_ptr"], t["reach_up_idx"], R)
+    np.testing.assert_array_equal(lp, lp2)
+    np.testing.assert_array_equal(lr, lr2)
+    lv, lp3, lr3 = T.levels(t["reach_up_ptr"], t["reach_up_idx"])
+    np.testing.assert_array_equal(lp, lp3)
+    np.testing.assert_array_equal(lr, lr3)
+
+
+def test_c1_has_about_3000_levels():
+    from oracle import troute_oracle as O
+
+    t = synth.make_tree(synth.C1_SEED, 550_000, 2_700_000)
+    lv, lp, lr = T.levels(t["reach_up_ptr"], t["reach_up_idx"])
+    assert len(lp) - 1 == 3016 and len(t["reach_seg_start"]) == 1_099_999
+    b = O.gen_tree(O.C1_SEED, 550_000, 2_700_000)
+    assert b["reach_up_idx"].tobytes() == t["reach_up_idx"].tobytes()
+    assert b["reach_seg_len"].tobytes() == t["reach_seg_len"].tobytes()

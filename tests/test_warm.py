@@ -243,11 +243,31 @@ def test_warm_start_needs_a_model():
         T.Network(c["topo"], c["params"], cfg=tight_cfg(warm_start=1, mapping=2))
 
 
+def _dev_stats(x, y):
+    r = np.abs(x - y) / np.maximum(np.abs(y), 1e-12)
+    return float(np.median(r)), float(np.quantile(r, 0.99)), float(r.max())
+
+
 def test_ab_trained_network_against_plain_on_a_fresh_network():
     """Train on pairs of plain runs of one network, route a fresh-seed network
-    with and without the model: iterations, fallback rate and the deviation of
-    discharge from the plain form, beside the plain form's own sensitivity to
-    a one-ulp change of its initial depth (the oracle)."""
+    with and without the model (24 steps, rtol 1e-8):
+
+    - the trained network must save at least 15 % of the secant passes per
+      solve, with fewer than half of its starts falling back;
+    - the plain GPU history equals the oracle's (correctly rounded powers) bit
+      for bit;
+    - the learned form's deviation from the plain form (median and 99th
+      percentile of |dq|/q over the whole history) must not exceed twice that
+      of a perfect predictor: the oracle started from the plain run's own
+      converged depth of every solve, with the same bracket and pass limit.
+      The reference secant stops where its bracket collapses (its two
+      residuals use different X clamps, troute_mc_final.cu:86 vs :105), so any
+      start other than the plain one lands elsewhere; the perfect predictor
+      already deviates by more than 1e-6 at the 99th percentile, which is why
+      "discharge within 1e-6 of the plain form" is out of reach for any warm
+      start, learned or not. The plain form's own one-ulp sensitivity (initial
+      depth moved by one ulp; C-library vs correctly rounded pow) is printed
+      beside it."""
     _, _, buf = record_pairs("tree:100000", 31, 24)
     m = T.WarmModel(5)
     loss = m.fit(buf.data_ptr(), buf.shape[0], epochs=4, batch=8192, lr=2e-3, seed=6)
@@ -265,9 +285,29 @@ def test_ab_trained_network_against_plain_on_a_fresh_network():
     n_solve = plain["solves"] - plain["early_exits"]
     ip, iw = plain["iterations"] / n_solve, warm["iterations"] / n_solve
     fb = warm["warm_fallback"] / max(1, warm["warm_used"])
-    qa, qb = out[1][1], out[0][1]
-    rel = np.abs(qa - qb) / np.maximum(np.abs(qb), 1e-12)
-    print(f"\nA/B tree:100000 seed 32, 24 steps: plain {ip:.3f} it/solve, warm {iw:.3f} it/solve, "
-          f"fallback {fb:.3f}, |dq|/q vs plain: median {np.median(rel):.2e}, p99 {np.quantile(rel, 0.99):.2e}")
+    qw, qp = out[1][1], out[0][1]
+    learned = _dev_stats(qw, qp)
+
+    def oracle_hist(mode=1, d0=None, **kw):
+        with O.pow_mode(mode):
+            return O.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"] if d0 is None else d0, c["rl0"],
+                                tol=TIGHT, history=True, threads=16, **kw)
+
+    with O.pow_mode(1):
+        o = O.route_tree(c["topo"], c["params"], c["qlat"], c["q0"], c["d0"], c["rl0"], tol=TIGHT, history=True,
+                         depth_history=True, threads=16)
+    np.testing.assert_array_equal(qp, o["q_hist"])
+    perfect = _dev_stats(oracle_hist(warm_start=o["d_hist"], warm_delta=0.05, warm_k=16)["q_hist"], o["q_hist"])
+    ulp = _dev_stats(oracle_hist(d0=np.nextafter(c["d0"], np.inf))["q_hist"], o["q_hist"])
+    libm = _dev_stats(oracle_hist(mode=0)["q_hist"], o["q_hist"])
+    print(f"\nA/B tree:100000 seed 32, 24 steps: plain {ip:.3f} it/solve, warm {iw:.3f} it/solve "
+          f"({100 * (1 - iw / ip):.1f} % fewer), fallback {fb:.3f}\n"
+          f"  |dq|/q vs plain (median, p99, max): learned {learned[0]:.2e} {learned[1]:.2e} {learned[2]:.2e}; "
+          f"perfect predictor {perfect[0]:.2e} {perfect[1]:.2e} {perfect[2]:.2e}; "
+          f"plain with initial depth +1 ulp {ulp[0]:.2e} {ulp[1]:.2e} {ulp[2]:.2e}; "
+          f"plain with C-library pow {libm[0]:.2e} {libm[1]:.2e} {libm[2]:.2e}")
     assert warm["warm_used"] > 0.9 * n_solve
     assert fb < 0.5
+    assert iw <= 0.85 * ip
+    assert learned[0] <= 2.0 * perfect[0] and learned[1] <= 2.0 * perfect[1]
+    assert perfect[1] > 1e-6
