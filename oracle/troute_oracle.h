@@ -154,6 +154,24 @@ typedef struct oracle_diff_reach {
 int oracle_diffusive_tridiag(const oracle_diff_reach* rp, const float* dx, const float* diffusivity,
                              const float* qp_prev, float* qp_out, int n_reaches, int max_nodes);
 
+/* Matrix-form linearised MC (oracle_matrix.c; linear_mc_matrix.cu): a CSR
+ * matrix whose arrays the oracle allocates (oracle_csr_free releases them). */
+typedef struct oracle_csr {
+    int n;
+    int* ptr;   /* [n + 1] */
+    int* col;   /* [nnz] */
+    float* val; /* [nnz] */
+} oracle_csr;
+void oracle_matrix_coeffs(const oracle_chparams_f32* params, int n, float dt, float* c1, float* c2, float* c3,
+                          float* c4oq);
+/* Returns 0, 2 (out of memory) or 3 (a reach not numbered after its upstream reaches). */
+int oracle_matrix_build(int R, const int* up_ptr, const int* up_idx, const float* c1, const float* c2,
+                        const float* c3, const float* c4oq, float tol, oracle_csr* PQ, oracle_csr* Pq);
+void oracle_csr_free(oracle_csr* m);
+void oracle_matrix_step(const oracle_csr* PQ, const oracle_csr* Pq, const float* x, const float* ql, float* y);
+int oracle_matrix_route(const oracle_csr* PQ, const oracle_csr* Pq, const float* qlat_ts, const float* q0,
+                        float* q_final, int n_ts);
+
 /* Seeded synthetic inputs (oracle_gen.c), byte for byte the product
  * generator's: tree topology (returns 0, or 1 for bad sizes, 2 out of memory),
  * channel parameters, lateral inflow [n_ts][n_segments] for steps t0..,

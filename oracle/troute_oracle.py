@@ -92,6 +92,14 @@ def oracle():
         L.oracle_gen_member.restype = None
         L.oracle_levels.argtypes = [C.c_int, _P, _P, _P, _P]
         L.oracle_levels.restype = C.c_int
+        L.oracle_matrix_coeffs.argtypes = [_P, C.c_int, C.c_float] + [_P] * 4
+        L.oracle_matrix_coeffs.restype = None
+        L.oracle_matrix_build.argtypes = [C.c_int, _P, _P, _P, _P, _P, _P, C.c_float, _P, _P]
+        L.oracle_matrix_build.restype = C.c_int
+        L.oracle_csr_free.argtypes = [_P]
+        L.oracle_csr_free.restype = None
+        L.oracle_matrix_route.argtypes = [_P, _P, _P, _P, _P, C.c_int]
+        L.oracle_matrix_route.restype = C.c_int
         _ORC = L
     return _ORC
 
@@ -137,6 +145,12 @@ def ref():
         L.ref_cpu_diffusive_tridiag.argtypes = [_P] * 6 + [C.c_int]
         L.ref_cpu_diffusive_tridiag.restype = None
         L.ref_diffusive_max_nodes.restype = C.c_int
+        L.ref_matrix_coeffs.argtypes = [_P, C.c_int, C.c_float] + [_P] * 4
+        L.ref_matrix_coeffs.restype = None
+        L.ref_matrix_build.argtypes = [C.c_int, _P, _P, _P, _P, _P, _P, C.c_float, _P, _P]
+        L.ref_matrix_build.restype = None
+        L.ref_matrix_fetch.argtypes = [C.c_int, _P, _P, _P]
+        L.ref_matrix_fetch.restype = None
         _REF = L
     return _REF
 
@@ -472,4 +486,82 @@ def ensemble_member(w: dict, member: int, seed: int = MEMBER_SEED) -> dict:
     p["ncc"] *= nf
     out = dict(w)
     out.update(params=p, qlat=w["qlat"] * qf[None, :], qfac=qf, nfac=nf, member=member)
+    return out
+
+
+# --------------------------------------------------------------------------- matrix form
+class CSR(C.Structure):
+    _fields_ = [("n", C.c_int), ("ptr", C.POINTER(C.c_int)), ("col", C.POINTER(C.c_int)),
+                ("val", C.POINTER(C.c_float))]
+
+
+def matrix_coeffs(params_f32, dt=300.0, use_ref=False):
+    """Matrix-form coefficients (C1, C2, C3, C4/ql) at X = 0.25 per reach: the
+    oracle's restatement of compute_mc_coeffs_cpu or (use_ref) the reference's own."""
+    p = _params_f32(params_f32)
+    n = p.shape[0]
+    c = [np.zeros(n, np.float32) for _ in range(4)]
+    f = ref().ref_matrix_coeffs if use_ref else oracle().oracle_matrix_coeffs
+    f(_ptr(p), n, float(dt), *(_ptr(x) for x in c))
+    return c
+
+
+def _csr_arrays(m: CSR):
+    n = m.n
+    ptr = np.ctypeslib.as_array(m.ptr, shape=(n + 1,)).copy()
+    nnz = int(ptr[-1])
+    col = np.ctypeslib.as_array(m.col, shape=(max(nnz, 1),))[:nnz].copy()
+    val = np.ctypeslib.as_array(m.val, shape=(max(nnz, 1),))[:nnz].copy()
+    return ptr, col, val
+
+
+def matrix_build(up_ptr, up_idx, coeffs, tol=1e-7, use_ref=False):
+    """The truncated propagation matrices ((ptr, col, val) of P_Q, of P_q): the
+    oracle's restatement of build_propagation_matrices or (use_ref) the
+    reference's own."""
+    up_ptr = np.ascontiguousarray(up_ptr, np.int32)
+    up_idx = np.ascontiguousarray(up_idx if len(up_idx) else [0], np.int32)
+    R = up_ptr.size - 1
+    cs = [np.ascontiguousarray(c, np.float32) for c in coeffs]
+    if use_ref:
+        nq, nl = C.c_int(), C.c_int()
+        ref().ref_matrix_build(R, _ptr(up_ptr), _ptr(up_idx), *(_ptr(c) for c in cs), float(tol), C.byref(nq),
+                               C.byref(nl))
+        out = []
+        for which, nnz in ((0, nq.value), (1, nl.value)):
+            ptr, col, val = np.zeros(R + 1, np.int32), np.zeros(max(nnz, 1), np.int32), np.zeros(max(nnz, 1), np.float32)
+            ref().ref_matrix_fetch(which, _ptr(ptr), _ptr(col), _ptr(val))
+            out.append((ptr, col[:nnz], val[:nnz]))
+        return tuple(out)
+    PQ, Pq = CSR(), CSR()
+    rc = oracle().oracle_matrix_build(R, _ptr(up_ptr), _ptr(up_idx), *(_ptr(c) for c in cs), float(tol), C.byref(PQ),
+                                      C.byref(Pq))
+    if rc:
+        raise ValueError(f"oracle_matrix_build: {rc}")
+    try:
+        return _csr_arrays(PQ), _csr_arrays(Pq)
+    finally:
+        oracle().oracle_csr_free(C.byref(PQ))
+        oracle().oracle_csr_free(C.byref(Pq))
+
+
+def matrix_route(PQ, Pq, qlat_ts, q0):
+    """The matrix form routed n_ts steps (the reference's fused kernel's
+    arithmetic, oracle_matrix_step); returns the final discharge."""
+    keep = []
+
+    def csr(m):
+        ptr, col, val = (np.ascontiguousarray(m[0], np.int32), np.ascontiguousarray(m[1] if len(m[1]) else [0], np.int32),
+                         np.ascontiguousarray(m[2] if len(m[2]) else [0], np.float32))
+        keep.extend((ptr, col, val))
+        return CSR(ptr.size - 1, ptr.ctypes.data_as(C.POINTER(C.c_int)), col.ctypes.data_as(C.POINTER(C.c_int)),
+                   val.ctypes.data_as(C.POINTER(C.c_float)))
+
+    a, b = csr(PQ), csr(Pq)
+    ql = np.ascontiguousarray(qlat_ts, np.float32)
+    q0 = np.ascontiguousarray(q0, np.float32)
+    out = np.zeros(a.n, np.float32)
+    rc = oracle().oracle_matrix_route(C.byref(a), C.byref(b), _ptr(ql), _ptr(q0), _ptr(out), int(ql.shape[0]))
+    if rc:
+        raise MemoryError("oracle_matrix_route")
     return out

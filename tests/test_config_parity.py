@@ -3,9 +3,11 @@ FP64 CPU oracle (the reference's algorithm restated; run here with all host
 threads, level-parallel, which does not change its results), with the
 maximum relative error on discharge reported for every config:
 
-- at the reference's tolerance (rtol 0.01), against the oracle with the C
-  library's pow() -- the reference's own arithmetic, bit-identical to its
-  compiled routine: max relative error below 1e-10;
+- at the reference's tolerance (rtol 0.01): bit-identical to the oracle
+  with correctly rounded powers; against the oracle with the C library's
+  pow() -- the reference's own arithmetic, bit-identical to its compiled
+  routine -- at most one segment per million above 1e-10 relative and none
+  above 1e-9 (libm_bar);
 - at rtol 1e-8, against the oracle with correctly rounded powers (the
   arithmetic the GPU uses): bit-identical (max relative error 0), also for
   the learned warm start replayed from the starting depths the GPU used;
@@ -51,6 +53,22 @@ def max_rel(a, b):
 
 def report(config, tol, oracle, err):
     print(f"\nPARITY {config} rtol={tol[0]:g} {oracle} max_rel={err:.3e}")
+
+
+def libm_bar(config, got, libm_q):
+    """At the reference tolerance against the C-library-pow oracle (the
+    reference's arithmetic): at most one segment per million above 1e-10
+    relative and none above 1e-9. The library's powers are correctly rounded
+    and libm misrounds ~0.2 % of them by one ulp; where the secant's update
+    cancels (small flows) that ulp can grow to ~5e-10 relative (c1: one segment
+    of 2.7 M at 0.0017 m3/s, iteration counts unchanged). The strict check is
+    the bit-identical one against the correctly rounded oracle."""
+    got, libm_q = np.asarray(got), np.asarray(libm_q)
+    den = np.maximum(np.abs(libm_q), 1e-300)
+    rel = np.where(got == libm_q, 0.0, np.abs(got - libm_q) / den)
+    n_over = int((rel > 1e-10).sum())
+    print(f"\nPARITY {config} rtol=0.01 libm segments over 1e-10: {n_over} of {rel.size}")
+    assert rel.max() <= 1e-9 and n_over <= max(1, rel.size // 1_000_000)
 
 
 def oracle(net, params, qlat, tol, mode, **kw):
@@ -102,9 +120,10 @@ def member_params(c1, nf, m):
 def test_c1(c1):
     args = (c1["topo"], c1["params"], c1["qlat"], c1["q0"], c1["d0"], c1["rl0"])
     g = T.route_tree(*args, cfg=cfg_of(REF))
-    e = max_rel(g["q"], oracle(c1, c1["params"], c1["qlat"], REF, 0)["q"])
-    report("c1", REF, "libm", e)
-    assert e < 1e-10
+    o0 = oracle(c1, c1["params"], c1["qlat"], REF, 0)
+    report("c1", REF, "libm", max_rel(g["q"], o0["q"]))
+    libm_bar("c1", g["q"], o0["q"])
+    np.testing.assert_array_equal(g["q"], oracle(c1, c1["params"], c1["qlat"], REF, 1)["q"])
     g = T.route_tree(*args, cfg=cfg_of(TIGHT))
     o1 = oracle(c1, c1["params"], c1["qlat"], TIGHT, 1)
     report("c1", TIGHT, "crpow", max_rel(g["q"], o1["q"]))
@@ -118,47 +137,50 @@ def test_c2():
     nets = synth.basins(seed=1002, n_trees=256)
     S = sum(n["topo"]["n_segments"] for n in nets)
     qlat = synth.make_qlat(1002, S, 1)
-    for tol, modes in ((REF, (0,)), (TIGHT, (1,))):
+    for tol, modes in ((REF, (0, 1)), (TIGHT, (1,))):
         with T.Network([n["topo"] for n in nets], [n["params"] for n in nets], cfg=cfg_of(tol)) as b:
             b.set_state(np.full(S, synth.Q0), np.full(S, synth.D0),
                         np.concatenate([np.full(len(n["topo"]["reach_seg_start"]), synth.Q0) for n in nets]))
             b.run(qlat)
             q = b.get_state()[0]
         for mode in modes:
-            worst, off = 0.0, 0
+            worst, off, parts = 0.0, 0, []
             for n in nets:
                 Sn = n["topo"]["n_segments"]
                 net = dict(n, q0=np.full(Sn, synth.Q0), d0=np.full(Sn, synth.D0),
                            rl0=np.full(len(n["topo"]["reach_seg_start"]), synth.Q0))
                 o = oracle(net, n["params"], np.ascontiguousarray(qlat[:, off:off + Sn]), tol, mode)
                 worst = max(worst, max_rel(q[off:off + Sn], o["q"]))
-                if tol is TIGHT and mode == 1:
+                parts.append(o["q"])
+                if mode == 1:
                     np.testing.assert_array_equal(q[off:off + Sn], o["q"])
                 off += Sn
             report("c2", tol, "libm" if mode == 0 else "crpow", worst)
-            if tol is REF:
-                assert worst < 1e-10
+            if mode == 0:
+                libm_bar("c2", q, np.concatenate(parts))
 
 
 def test_c4(c1, members):
     qf, nf = members
     S = c1["topo"]["n_segments"]
     M = 64
-    for tol, modes in ((REF, (0,)), (TIGHT, (1,))):
+    for tol, modes in ((REF, (0, 1)), (TIGHT, (1,))):
         with T.Network.ensemble(c1["topo"], c1["params"], M, n_scale=nf, qlat_scale=qf, cfg=cfg_of(tol)) as net:
             net.set_state(np.tile(c1["q0"], M), np.tile(c1["d0"], M), np.tile(c1["rl0"], M))
             net.run(c1["qlat"][:1])
             q = net.get_state()[0]
         for mode in modes:
-            worst = 0.0
+            worst, parts = 0.0, []
             for m in MEMBERS:
                 o = oracle(c1, member_params(c1, nf, m), c1["qlat"][:1] * qf[m][None, :], tol, mode)
                 worst = max(worst, max_rel(q[m * S:(m + 1) * S], o["q"]))
-                if tol is TIGHT and mode == 1:
+                parts.append(o["q"])
+                if mode == 1:
                     np.testing.assert_array_equal(q[m * S:(m + 1) * S], o["q"])
             report(f"c4 members {MEMBERS}", tol, "libm" if mode == 0 else "crpow", worst)
-            if tol is REF:
-                assert worst < 1e-10
+            if mode == 0:
+                libm_bar(f"c4 members {MEMBERS}", np.concatenate([q[m * S:(m + 1) * S] for m in MEMBERS]),
+                         np.concatenate(parts))
 
 
 def test_c4w_warm_start_replays(c1, members, model):
