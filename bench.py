@@ -823,10 +823,35 @@ def run_ours(args, dist: Dist):
         print(json.dumps(line), flush=True)
 
 
+def _event_timed(torch, stream, fn, warmup: int, steps: int):
+    """Runs fn() warmup times, then times `steps` calls with CUDA events on
+    `stream` (synchronised on both sides); returns ms per call."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def _line(metric, value, unit, args, dist, ms, dtype, workload, extra):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": dist.world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded generator)", "config": {"workload": workload}}
+    out.update(extra)
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_linear(args, dist: Dist):
     """lin:<network>: the linearised-MC approximate mode (FP32, one persistent
     launch per run) on a single network; one bench step = one run of n_ts steps
-    from the carried-over discharge. Reported on its own metric line."""
+    from the carried-over discharge, timed with CUDA events. Reported on its
+    own metric line."""
     import torch
 
     import troute_gb300 as T
@@ -839,24 +864,169 @@ def run_linear(args, dist: Dist):
     coeffs = T.linear_coeffs(p32, w["dt"])
     ql = torch.from_numpy(w["qlat"].astype(np.float32)).to(dev)
     q = torch.from_numpy(w["q0"].astype(np.float32)).to(dev)
+    stream = torch.cuda.Stream(dev)   # a real stream (0 would mean the handle's own)
+    torch.cuda.synchronize(dev)
     net = T.LinearNetwork(w["topo"], coeffs)
-    for _ in range(args.warmup):
-        net.run_device(ql.data_ptr(), n_ts, q.data_ptr())
+    dist.barrier()
+    ms = dist.max(_event_timed(torch, stream, lambda: net.run_device(ql.data_ptr(), n_ts, q.data_ptr(),
+                                                                     stream=stream.cuda_stream),
+                               args.warmup, args.steps))
+    net.close()
+    value = S * n_ts * dist.world / (ms / 1e3)
+    _line("segment-steps/s, linearised MC (approximate mode, FP32)", value, UNIT, args, dist, ms, "f32",
+          f"{args.workload}: {S} segments, {n_ts} steps per bench step (one persistent dataflow launch), "
+          f"CUDA-event timed", {"config": {"workload": f"{args.workload}: {S} segments, {n_ts} steps per bench step",
+                                          "segments": S, "timesteps_per_step": n_ts}})
+
+
+def matrix_inputs(name: str, n_ts: int | None):
+    """The matrix form's reach-level network from a synthetic tree: reach r
+    takes parameter record r and inflow column r (as the reference's main()
+    reads its network files), initial discharge 0.1 m3/s."""
+    from troute_gb300 import synth
+
+    w = synth.network(name, n_ts=n_ts)
+    t = w["topo"]
+    R = len(t["reach_seg_start"])
+    p32 = np.ascontiguousarray(np.asarray(w["params"].view("<f8").reshape(-1, 8)[:R], np.float32))
+    ql = np.ascontiguousarray(w["qlat"][:, :R], np.float32)
+    return t["reach_up_ptr"], t["reach_up_idx"], p32, ql, np.full(R, 0.1, np.float32), w["dt"]
+
+
+def run_matrix(args, dist: Dist):
+    """mat:<network>: the matrix-form linear MC (FP32): one bench step = one
+    n_ts-step run (a graph of n_ts fused step launches) over the reach-level
+    form of the network, timed with CUDA events. HBM roofline: every step
+    streams both matrices (8 B per stored entry), their row pointers, the
+    step's lateral inflow and writes the discharge."""
+    import torch
+
+    import troute_gb300 as T
+    from oracle import troute_oracle as O
+
+    dev = torch.device("cuda", dist.local if dist.world > 1 else 0)
+    torch.cuda.set_device(dev)
+    name = args.workload.split(":", 1)[1]
+    up_ptr, up_idx, p32, ql_h, q0, dt = matrix_inputs(name, args.n_ts)
+    R, n_ts = len(q0), ql_h.shape[0]
+    coeffs = T.matrix_coeffs(p32, dt)
+    t0 = time.perf_counter()
+    net = T.MatrixNetwork(up_ptr, up_idx, coeffs)
+    build_s = time.perf_counter() - t0
+    ql = torch.from_numpy(ql_h).to(dev)
+    q = torch.from_numpy(q0.copy()).to(dev)
+    stream = torch.cuda.Stream(dev)   # a real stream (0 would mean the handle's own)
     torch.cuda.synchronize(dev)
     dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        net.run_device(ql.data_ptr(), n_ts, q.data_ptr())   # synchronous
-    el = dist.max(time.perf_counter() - t0)
+    ms = dist.max(_event_timed(torch, stream, lambda: net.run_device(ql.data_ptr(), n_ts, q.data_ptr(),
+                                                                     stream.cuda_stream), args.warmup, args.steps))
+    value = R * n_ts * dist.world / (ms / 1e3)
+    bytes_step = 8 * (net.nnz_Q + net.nnz_q) + 8 * (R + 1) + 12 * R
+    hbm_peak, kind = measured_peak_hbm()
+    achieved = bytes_step * n_ts / (ms / 1e3) / 1e9
+    # parity: 8 steps from the initial discharge against the oracle (the
+    # reference kernel's arithmetic on the same matrices), bit for bit
+    k = min(8, n_ts)
+    qa = torch.from_numpy(q0.copy()).to(dev)
+    net.run_device(ql.data_ptr(), k, qa.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize()
+    m = net.matrices()
+    want = O.matrix_route(m[0], m[1], ql_h[:k], q0)
+    got = qa.cpu().numpy()
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        O.matrix_route(m[0], m[1], ql_h[:2], q0)
+        el = time.perf_counter() - t0
+        cpu = {"value": R * 2 / el, "unit": "reach-steps/s", "cores": 1, "kind": "port",
+               "sample": f"2 steps of the {R}-reach network from the initial discharge, single thread (the oracle's "
+                         f"restatement of the reference's step on the same matrices; the reference's step runs only "
+                         f"on the GPU)", "host": host_cpu()}
     net.close()
-    value = S * n_ts * args.steps * dist.world / el
-    if dist.rank == 0:
-        print(json.dumps({"metric": "segment-steps/s, linearised MC (approximate mode, FP32)", "value": value,
-                          "unit": UNIT, "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
-                          "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
-                          "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-                          "config": {"workload": f"{args.workload}: {S} segments, {n_ts} steps per bench step, "
-                                                 f"host-timed synchronous runs", "segments": S}}), flush=True)
+    _line("reach-steps/s, matrix-form linear MC (approximate mode, FP32)", value, "reach-steps/s", args, dist, ms,
+          "f32", f"{args.workload}", {
+              "config": {"workload": f"{args.workload}: reach-level form of the {name} network ({R} reaches, one "
+                                     f"routing unit per reach), truncated propagation matrices at tol 1e-7 "
+                                     f"(P_Q {net.nnz_Q} entries, P_q {net.nnz_q}), {n_ts} steps per bench step",
+                         "reaches": R, "nnz_PQ": net.nnz_Q, "nnz_Pq": net.nnz_q, "timesteps_per_step": n_ts,
+                         "build_s": round(build_s, 2),
+                         "l2": f"matrices {8 * (net.nnz_Q + net.nnz_q) / 1e6:.0f} MB streamed per step"},
+              "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                           "frac": achieved / hbm_peak, "traffic": None,
+                           "alg_bytes_per_step": bytes_step,
+                           "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured" else "fallback"},
+              "parity": {"steps": k, "bit_identical_to_oracle": bool(np.array_equal(got, want))},
+              "cpu_baseline": cpu, "gpu_launches": n_ts * args.steps})
+
+
+def run_diffusive(args, dist: Dist):
+    """diff:<reaches>: the diffusive-wave tridiagonal step on reaches with the
+    reference's benchmark distributions (20-99 nodes of at most 500, theta
+    0.6, dt 60 s, dx U(100, 600) m, diffusivity U(10, 110), discharge
+    U(1, 51)); one bench step = one launch over all reaches, CUDA-event timed.
+    HBM roofline: per computational node dx, diffusivity and the previous
+    discharge are read and the new discharge written (16 B)."""
+    import torch
+
+    import troute_gb300 as T
+    from oracle import troute_oracle as O
+
+    dev = torch.device("cuda", dist.local if dist.world > 1 else 0)
+    torch.cuda.set_device(dev)
+    n = int(args.workload.split(":", 1)[1])
+    M = 500
+    rng = np.random.default_rng(2027)
+    rp = np.zeros(n, T.api.DIFF_REACH_DTYPE)
+    rp["ncomp"] = rng.integers(20, 100, n)
+    rp["theta"] = 0.6
+    rp["dtini"] = 60.0
+    dx = rng.uniform(100.0, 600.0, (n, M)).astype(np.float32)
+    df = rng.uniform(10.0, 110.0, (n, M)).astype(np.float32)
+    qp = rng.uniform(1.0, 51.0, (n, M)).astype(np.float32)
+    nodes = int(rp["ncomp"].sum())
+    g = {k: torch.from_numpy(v).to(dev) for k, v in (("dx", dx), ("df", df), ("qp", qp))}
+    g["rp"] = torch.from_numpy(rp.view(np.uint8)).to(dev)
+    out = torch.zeros((n, M), dtype=torch.float32, device=dev)
+    scratch = torch.empty(2 * n * M, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(dev)   # a real stream (0 would mean the handle's own)
+    torch.cuda.synchronize(dev)
+    L = T.lib()
+
+    def step():
+        rc = L.troute_diffusive_tridiag_device(g["rp"].data_ptr(), g["dx"].data_ptr(), g["df"].data_ptr(), None,
+                                               g["qp"].data_ptr(), out.data_ptr(), n, M, scratch.data_ptr(),
+                                               stream.cuda_stream)
+        if rc:
+            raise RuntimeError(L.troute_last_error())
+
+    dist.barrier()
+    ms = dist.max(_event_timed(torch, stream, step, args.warmup, args.steps))
+    value = nodes * dist.world / (ms / 1e3)
+    hbm_peak, kind = measured_peak_hbm()
+    achieved = 16.0 * nodes / (ms / 1e3) / 1e9
+    sample = min(n, 2000)
+    want = O.diffusive_tridiag(rp[:sample], dx[:sample], df[:sample], qp[:sample])
+    got = out.cpu().numpy()[:sample]
+    mask = np.arange(M)[None, :] < rp["ncomp"][:sample, None]
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        O.diffusive_tridiag(rp[:sample], dx[:sample], df[:sample], qp[:sample])
+        el = time.perf_counter() - t0
+        cpu = {"value": int(rp["ncomp"][:sample].sum()) / el, "unit": "node-steps/s", "cores": 1, "kind": "port",
+               "sample": f"the first {sample} reaches, single thread (the oracle's restatement of "
+                         f"cpu_diffusive_tridiag, bit-identical to it)", "host": host_cpu()}
+    _line("node-steps/s, diffusive-wave tridiagonal step (FP32)", value, "node-steps/s", args, dist, ms, "f32",
+          args.workload, {
+              "config": {"workload": f"{args.workload}: {n} reaches x {M} node slots, {nodes} computational nodes "
+                                     f"(20-99 per reach), one launch per bench step", "reaches": n, "nodes": nodes,
+                         "l2": f"inputs {3 * n * M * 4 / 1e9:.2f} GB (larger than L2)"},
+              "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                           "frac": achieved / hbm_peak, "traffic": None, "alg_bytes_per_node": 16,
+                           "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured" else "fallback"},
+              "parity": {"reaches_checked": sample, "bit_identical_to_oracle": bool(np.array_equal(got[mask],
+                                                                                                  want[mask]))},
+              "cpu_baseline": cpu, "gpu_launches": args.steps})
 
 
 def main():
@@ -867,6 +1037,10 @@ def main():
             run_reference(args, dist)
         elif args.workload.startswith("lin:"):
             run_linear(args, dist)
+        elif args.workload.startswith("mat:"):
+            run_matrix(args, dist)
+        elif args.workload.startswith("diff:"):
+            run_diffusive(args, dist)
         else:
             run_ours(args, dist)
     finally:

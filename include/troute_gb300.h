@@ -353,6 +353,40 @@ int troute_levels(int n_reaches, const int* reach_up_ptr, const int* reach_up_id
 /* Checks a topology; returns TROUTE_OK or TROUTE_ETOPO with a message. */
 int troute_validate(const troute_topo* topo);
 
+/* ---- matrix-form linearised MC (approximate mode) ----------------------- */
+/* The reference's matrix form (water-prediction/t-route/wavefront/
+ * linear_mc_matrix.cu, fused step of linear_mc_matrix_graph.cu:174-206): a
+ * reach-level network (one routing unit per reach) with fixed coefficients
+ * at X = 0.25 is routed as Q_new = P_Q Q_old + P_q qlat with the truncated
+ * propagation matrices P_Q = (I - C1 N)^-1 (C2 N + C3), P_q = (I - C1 N)^-1 C4
+ * (N: upstream adjacency), FP32. Reaches must be numbered upstream first. */
+typedef struct troute_matrix troute_matrix;
+/* C1, C2, C3, C4/ql per reach at X = 0.25 (compute_mc_coeffs_cpu,
+ * linear_mc_matrix.cu:56-86), evaluated on the device. */
+int troute_matrix_coeffs(const troute_chparams_f32* params, int n_reaches, double dt, float* c1, float* c2,
+                         float* c3, float* c4oq);
+/* Builds P_Q and P_q once on the host (build_propagation_matrices,
+ * linear_mc_matrix.cu:129-216; entries with |value| < tol dropped, the
+ * reference uses 1e-7) and uploads them. TROUTE_ETOPO when a reach is not
+ * numbered after its upstream reaches. */
+int troute_matrix_create(troute_matrix** h, int n_reaches, const int* reach_up_ptr, const int* reach_up_idx,
+                         const float* c1, const float* c2, const float* c3, const float* c4oq, float tol);
+int troute_matrix_destroy(troute_matrix* h);
+/* Sizes: reaches and stored entries of P_Q and P_q (any pointer may be NULL). */
+int troute_matrix_info(const troute_matrix* h, int* n_reaches, long long* nnz_Q, long long* nnz_q);
+/* Host copies of P_Q (which = 0) or P_q (1) in CSR: ptr [n_reaches + 1],
+ * col and val [nnz] (any pointer may be NULL). */
+int troute_matrix_get(const troute_matrix* h, int which, int* ptr, int* col, float* val);
+/* Routes n_ts steps on the device: qlat_ts [n_ts][n_reaches], q [n_reaches]
+ * in/out; asynchronous on `stream` (NULL: the handle's own). The run is
+ * recorded as a CUDA graph on first use and replayed while the buffers and
+ * n_ts stay the same. */
+int troute_matrix_run_device(troute_matrix* h, const float* qlat_ts_device, int n_ts, float* q_device, void* stream);
+/* One-shot host form: build, route n_ts steps from q0, return the discharge. */
+int troute_matrix_route(int n_reaches, const int* reach_up_ptr, const int* reach_up_idx, const float* c1,
+                        const float* c2, const float* c3, const float* c4oq, float tol, const float* qlat_ts,
+                        const float* q0, int n_ts, float* q_out);
+
 /* ---- linearised MC (approximate mode) --------------------------------- */
 /* The reference's linear form (water-prediction/t-route/wavefront/
  * linear_mc.cu): fixed per-segment coefficients C1, C2, C3, C4/ql from the

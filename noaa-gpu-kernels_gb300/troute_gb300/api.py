@@ -165,6 +165,13 @@ _SIGS = {
     "troute_linear_destroy": ([_P], _I),
     "troute_linear_run_device": ([_P, _P, _I, _P, C.c_longlong, _P], _I),
     "troute_linear_route": ([_P, _P, _P, _P, _P, _P, _P, _I, _P], _I),
+    "troute_matrix_coeffs": ([_P, _I, _D, _P, _P, _P, _P], _I),
+    "troute_matrix_create": ([_P, _I, _P, _P, _P, _P, _P, _P, C.c_float], _I),
+    "troute_matrix_destroy": ([_P], _I),
+    "troute_matrix_info": ([_P, _P, _P, _P], _I),
+    "troute_matrix_get": ([_P, _I, _P, _P, _P], _I),
+    "troute_matrix_run_device": ([_P, _P, _I, _P, _P], _I),
+    "troute_matrix_route": ([_I, _P, _P, _P, _P, _P, _P, C.c_float, _P, _P, _I, _P], _I),
     "troute_qlat_from_csv": ([C.c_char_p, _P, _I, _I, _I, _P, _P, _P], _I),
     "troute_write_forcings": ([C.c_char_p, _I, _I, _I, _P, _P, _P, _P], _I),
     "troute_read_network": ([C.c_char_p, _P], _I),
@@ -663,6 +670,76 @@ def linear_route(topo: dict, coeffs, qlat_ts, q0):
     _check(lib().troute_linear_route(C.byref(t[0]), *(_ptr(c) for c in cs), _ptr(ql), _ptr(q), int(ql.shape[0]),
                                      _ptr(out)))
     return out
+
+
+def matrix_coeffs(params_f32, dt: float = 300.0):
+    """Matrix-form coefficients (C1, C2, C3, C4/ql) at X = 0.25 per reach,
+    float32, computed on the device."""
+    p = _f32_params(params_f32)
+    n = p.shape[0]
+    c = [np.zeros(n, np.float32) for _ in range(4)]
+    _check(lib().troute_matrix_coeffs(_ptr(p), n, float(dt), *(_ptr(x) for x in c)))
+    return c
+
+
+def matrix_route(up_ptr, up_idx, coeffs, qlat_ts, q0, tol: float = 1e-7):
+    """The matrix form on the GPU, one shot: reach-level upstream CSR (reaches
+    numbered upstream first), coefficients, lateral inflow [n_ts][n_reaches]
+    and initial discharge -> final discharge (float32)."""
+    up_ptr, up_idx = _i32(up_ptr), _i32(up_idx if len(up_idx) else np.zeros(1, np.int32))
+    R = up_ptr.size - 1
+    cs = [np.ascontiguousarray(c, np.float32) for c in coeffs]
+    ql = np.ascontiguousarray(qlat_ts, np.float32)
+    q = np.ascontiguousarray(q0, np.float32)
+    out = np.zeros(R, np.float32)
+    _check(lib().troute_matrix_route(R, _ptr(up_ptr), _ptr(up_idx), *(_ptr(c) for c in cs), float(tol), _ptr(ql),
+                                     _ptr(q), int(ql.shape[0]), _ptr(out)))
+    return out
+
+
+class MatrixNetwork:
+    """Persistent device form of the matrix-form linear MC (troute_matrix_*)."""
+
+    def __init__(self, up_ptr, up_idx, coeffs, tol: float = 1e-7):
+        up_ptr, up_idx = _i32(up_ptr), _i32(up_idx if len(up_idx) else np.zeros(1, np.int32))
+        cs = [np.ascontiguousarray(c, np.float32) for c in coeffs]
+        self._h = C.c_void_p()
+        _check(lib().troute_matrix_create(C.byref(self._h), up_ptr.size - 1, _ptr(up_ptr), _ptr(up_idx),
+                                          *(_ptr(c) for c in cs), float(tol)))
+        R, nq, nl = _I(), C.c_longlong(), C.c_longlong()
+        _check(lib().troute_matrix_info(self._h, C.byref(R), C.byref(nq), C.byref(nl)))
+        self.n_reaches, self.nnz_Q, self.nnz_q = R.value, nq.value, nl.value
+
+    def matrices(self):
+        """((ptr, col, val) of P_Q, (ptr, col, val) of P_q), host copies."""
+        out = []
+        for which, nnz in ((0, self.nnz_Q), (1, self.nnz_q)):
+            ptr = np.zeros(self.n_reaches + 1, np.int32)
+            col, val = np.zeros(max(nnz, 1), np.int32), np.zeros(max(nnz, 1), np.float32)
+            _check(lib().troute_matrix_get(self._h, which, _ptr(ptr), _ptr(col), _ptr(val)))
+            out.append((ptr, col[:nnz], val[:nnz]))
+        return tuple(out)
+
+    def run_device(self, qlat_dev_ptr: int, n_ts: int, q_dev_ptr: int, stream: int = 0):
+        _check(lib().troute_matrix_run_device(self._h, C.c_void_p(qlat_dev_ptr), int(n_ts), C.c_void_p(q_dev_ptr),
+                                              C.c_void_p(stream)))
+
+    def close(self):
+        if self._h:
+            lib().troute_matrix_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 DIFF_REACH_DTYPE = np.dtype([("ncomp", "<i4"), ("theta", "<f4"), ("dtini", "<f4")])
