@@ -22,13 +22,19 @@
 //      round(z + (delta + z e ln x)) and pow(x, fl(5/3)) =
 //      round(y z + (err(y z) + y delta + y z e' ln x)), each scaled back by
 //      2^(2k), 2^(5k) (exact).
-// The rounding of step 4 is therefore the correctly rounded result except when
-// the exact value lies within ~2^-74 relative of a rounding midpoint (the
+// The sums of step 4 are within ~2^-74 relative of the exact values (the
 // ~1e-16 exponent-offset term is formed from the seed's single-precision
 // log2, and on the device for x in [2^-9, 2^9) in single precision: ~2^-24
-// of it). Host and device forms agree on all but ~1e-7 of arguments. The C
-// library's pow() (glibc) is not correctly rounded: it differs from these
-// results by one ulp on ~0.2 % of arguments.
+// of it). Their rounding is checked (Ziv's rounding test): each sum s = a + c
+// is split exactly into s + err (Fast2Sum, |a| >= |c|), and when |err| comes
+// within 2^-68 relative of half an ulp of s -- a rounding midpoint the
+// computed sum may be on the wrong side of -- both powers are recomputed with
+// one more Newton step (z within ~2^-51, z + delta within ~2^-100) and the
+// offset terms from a double-precision log. That happens for ~1 argument in
+// 2^14; the results are then the correctly rounded values except within
+// ~2^-95 of a midpoint (never met in the parity runs, ~10^10 evaluations).
+// The C library's pow() (glibc) is not correctly rounded: it differs from
+// these results by one ulp on ~0.2 % of arguments.
 // Only IEEE operations and explicit fma() are used, so compiling without
 // implicit FMA contraction does not change these results.
 #pragma once
@@ -127,6 +133,22 @@ CRPOW_HD double crpow_scale(double v, int n)
 constexpr double kFl23Minus23 = -3.700743415417188e-17;
 constexpr double kFl53Minus53 = 7.401486830834377e-17;
 
+// Whether s = fl(a + c), with err = (a + c) - s exact, may round differently
+// from a value within 2^-68 s of a + c: |err| above (1 - 2^-15) ulp(s) / 2,
+// compared on the integer pipe (non-negative doubles order like their bit
+// patterns); a power of two (the spacing changes at s) or a tiny s always
+// counts as uncertain.
+CRPOW_HD bool crpow_near_midpoint(double s, double err)
+{
+    const uint64_t sb = crpow_bits(s);
+    const uint64_t eb = crpow_bits(err) & 0x7FFFFFFFFFFFFFFFull;
+    const uint64_t es = (sb >> 52) & 0x7FF;
+    if ((sb & 0x000FFFFFFFFFFFFFull) == 0 || es < 64) return true;
+    // (1 - 2^-15) ulp(s) / 2 = 2^(es - 1077) (2 - 2^-14): biased exponent es - 54
+    const uint64_t thr = ((es - 54) << 52) | 0x000FFFC000000000ull;
+    return eb > thr;
+}
+
 // x^fl(2/3) and x^fl(5/3), both correctly rounded (see above). x < 0 gives NaN,
 // x = 0 gives 0, +inf gives +inf, NaN propagates, like pow().
 CRPOW_HD void pow23_53(double x, double* p23, double* p53)
@@ -202,10 +224,38 @@ CRPOW_HD void pow23_53(double x, double* p23, double* p53)
     const double lnx = ((double)log2y + 3.0 * (double)k) * 0.6931471805599453;
     const double c2 = kFl23Minus23 * lnx, c5 = kFl53Minus53 * lnx;
 #endif
-    const double z23 = z + (delta + z * c2);
+    const double a23 = delta + z * c2;
+    double z23 = z + a23;
     const double w0 = y * z;
     const double we = fma(y, z, -w0);
-    const double z53 = w0 + ((we + y * delta) + w0 * c5);
+    const double a53 = (we + y * delta) + w0 * c5;
+    double z53 = w0 + a53;
+    // rounding test (Fast2Sum: z >= |a23|, w0 >= |a53|, so the errors are exact)
+    if (crpow_near_midpoint(z23, a23 - (z23 - z)) || crpow_near_midpoint(z53, a53 - (z53 - w0))) {
+        // one more Newton step for r, the residual correction again, and the
+        // offset terms from a double-precision log of x
+        const double r3 = (r * r) * r;
+        const double g = fma(-y, r3, 1.0);
+        const double rr = fma(r * g, third, r);
+        const double zz = y * rr;
+        const double pp = zz * zz;
+        const double ppe = fma(zz, zz, -pp);
+        const double qq = zz * pp;
+        const double qqe = fma(zz, pp, -qq);
+        const double tt = zz * ppe;
+        const double dd = (qq - s) + ((qqe + tt) - se);
+        const double rr2 = rr * rr;
+        const double dl = -(dd * (rr2 * rr2)) * third;
+#if defined(__CUDA_ARCH__)
+        const double lnx = log(y) + (double)(3 * k) * 0.6931471805599453;
+#else
+        const double lnx = std::log(y) + (double)(3 * k) * 0.6931471805599453;
+#endif
+        z23 = zz + (dl + zz * (kFl23Minus23 * lnx));
+        const double ww = y * zz;
+        const double wwe = fma(y, zz, -ww);
+        z53 = ww + ((wwe + y * dl) + ww * (kFl53Minus53 * lnx));
+    }
     *p23 = crpow_scale(z23, 2 * k);
     *p53 = crpow_scale(z53, 5 * k);
 }

@@ -137,8 +137,7 @@ __global__ void __launch_bounds__(128) route_kernel(NetDev net, RunDev run)
                     const long long s = base + (long long)i * kLanes;
                     const double qdp = __ldcg(net.q + s);
                     const double dpp = __ldcg(net.d + s);
-                    double ql = __ldg(qlat_row + __ldg(net.qcol + s));
-                    if (net.qscale) ql *= __ldg(net.qscale + s);
+                    const double ql = __ldg(qlat_row + __ldg(&net.seg[s].qcol)) * __ldg(&net.seg[s].qscale);
                     const SegP sp = load_seg(net, s);
                     const double qup = (i == 0) ? qup_head : q_up_old;
                     const double quc = (i == 0) ? quc_head : q_up_new;

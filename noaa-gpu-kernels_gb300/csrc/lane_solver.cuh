@@ -34,8 +34,18 @@ constexpr int kSegSmemStride = 128;  // threads per block of the per-lane kernel
 
 __device__ __forceinline__ void stage_seg(const NetDev& net, long long s, double2* slot)
 {
+    const SegRec* r = net.seg + s;
 #pragma unroll
-    for (int k = 0; k < kParamPlanes; ++k) slot[k * kSegSmemStride] = __ldg(net.prm[k] + s);
+    for (int k = 0; k < kParamPlanes; ++k) slot[k * kSegSmemStride] = __ldg(r->p + k);
+}
+
+// Lateral inflow of segment s in the step whose inflow row is qlat_row: the
+// record's column and scale, read as one 16-byte load {scale, column | pad}.
+__device__ __forceinline__ double seg_inflow(const NetDev& net, long long s, const double* qlat_row)
+{
+    const double2 qs = __ldg(reinterpret_cast<const double2*>(&net.seg[s].qscale));
+    const int col = (int)(unsigned)(__double_as_longlong(qs.y) & 0xffffffffll);   // qcol, the low word
+    return __ldg(qlat_row + col) * qs.x;
 }
 
 __device__ __forceinline__ SegP staged_seg(const double2* slot)
@@ -93,8 +103,7 @@ __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const 
         L.s = L.base + (long long)L.i * kLanes;
         L.qdp = __ldcg(net.q + L.s);
         const double dpp = __ldcg(net.d + L.s);
-        L.ql = __ldg(qlat_row + __ldg(net.qcol + L.s));
-        if (net.qscale) L.ql *= __ldg(net.qscale + L.s);
+        L.ql = seg_inflow(net, L.s, qlat_row);
         stage_seg(net, L.s, slot);
         const SegP p = staged_seg(slot);
         L.qup = (L.i == 0) ? L.qup_head : L.q_up_old;

@@ -29,8 +29,9 @@ namespace tr {
 
 __device__ __forceinline__ SegP load_seg(const NetDev& net, long long s)
 {
-    const double2 a = __ldg(net.prm[0] + s), b = __ldg(net.prm[1] + s), c = __ldg(net.prm[2] + s);
-    const double2 e = __ldg(net.prm[3] + s), f = __ldg(net.prm[4] + s), g = __ldg(net.prm[5] + s);
+    const SegRec* r = net.seg + s;
+    const double2 a = __ldg(r->p + 0), b = __ldg(r->p + 1), c = __ldg(r->p + 2);
+    const double2 e = __ldg(r->p + 3), f = __ldg(r->p + 4), g = __ldg(r->p + 5);
     SegP p;
     p.dx = a.x; p.bw = a.y; p.twcc = b.x; p.n_ch = b.y; p.ncc = c.x; p.s0 = c.y;
     p.z = e.x; p.bfd = e.y; p.sq_s0 = f.x; p.sq2 = f.y; p.ck_fac = g.x; p.z2 = g.y;

@@ -9,7 +9,9 @@
 //     counter, outflow ring) is read coalesced by a warp working on a block;
 //   - segment i of lane k of block b lives at tile_off[b] + 32*i + k, so the
 //     warp's loads of "segment i of every reach" are one 256-byte line per
-//     double plane; parameters are six double2 planes (vector loads);
+//     double plane; a segment's parameters, inflow column and inflow scale
+//     are one 128-byte record (SegRec: one L2 line per solve, whatever the
+//     order in which the per-lane kernels take (reach, step) items);
 //   - q, depth, velocity: one double plane each, updated in place each step;
 //   - reach outflow: a [4][reaches] ring indexed by step % 4.
 #include <cuda_runtime.h>
@@ -181,9 +183,9 @@ struct troute_handle {
     long long steps_done = 0;
     bool broken = false;
 
-    DBuf<double2> prm[kParamPlanes];
-    DBuf<int> qcol, nseg, block_level, lb_ptr_d, up_ptr, up_idx, down, done, step_base;
-    DBuf<double> qscale, q, d, v, ring, tmp, qlat_buf, hist;
+    DBuf<SegRec> seg;
+    DBuf<int> nseg, block_level, lb_ptr_d, up_ptr, up_idx, down, done, step_base;
+    DBuf<double> q, d, v, ring, tmp, qlat_buf, hist;
     DBuf<long long> tile_off, seg_map_d, reach_map_d;
     DBuf<unsigned long long> wave_ptr, wave_ptr_tail, ticket, rq_ctr;
     unsigned long long n_tickets = 0, n_tickets_tail = 0;
@@ -217,9 +219,7 @@ struct troute_handle {
         n.n_levels = n_levels;
         n.n_reach_int = R_int;
         n.n_seg_int = S_int;
-        for (int i = 0; i < kParamPlanes; ++i) n.prm[i] = prm[i].p;
-        n.qcol = qcol.p;
-        n.qscale = qscale.p;
+        n.seg = seg.p;
         n.nseg = nseg.p;
         n.tile_off = tile_off.p;
         n.block_level = block_level.p;
@@ -239,10 +239,10 @@ struct troute_handle {
     {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (graph) cudaGraphDestroy(graph);
-        for (auto& b : prm) b.release();
-        qcol.release(); nseg.release(); block_level.release(); lb_ptr_d.release();
+        seg.release();
+        nseg.release(); block_level.release(); lb_ptr_d.release();
         up_ptr.release(); up_idx.release(); down.release(); done.release(); step_base.release();
-        qscale.release(); q.release(); d.release(); v.release(); ring.release(); tmp.release();
+        q.release(); d.release(); v.release(); ring.release(); tmp.release();
         qlat_buf.release(); hist.release(); tile_off.release(); seg_map_d.release();
         reach_map_d.release(); wave_ptr.release(); wave_ptr_tail.release(); ticket.release(); stats.release();
         rq_ctr.release(); df_cnt.release(); df_rq.release(); df_heads.release(); df_rh.release();
@@ -292,22 +292,33 @@ struct Layout {
     int R_user = 0, S_user = 0, n_levels = 0, NB = 0, R_int = 0, n_heads = 0, R_real = 0;
     long long S_int = 0;  // tiles + 1 trash slot
     std::vector<int> user_seg_start, user_seg_len;
-    std::vector<int> lb_ptr, block_level, nseg, up_ptr, up_idx, down_i, qcol;
+    std::vector<int> lb_ptr, block_level, nseg, up_ptr, up_idx, down_i;
     std::vector<long long> tile_off, seg_map, reach_map;  // seg_map: -1 for uncovered segments
     std::vector<int2> heads;
-    std::vector<double2> planes[kParamPlanes];
-    std::vector<double> qscale;  // empty: no scaling
+    std::vector<SegRec> recs;    // parameters, inflow column and scale per tile slot
 };
 
-static void put_params(Layout& Lt, long long t, const troute_chparams& c)
+// A tile slot's record: derived parameters, inflow column, inflow scale.
+static void put_params(Layout& Lt, long long t, const troute_chparams& c, int qcol, double qscale)
 {
     const SegP p = derive_seg(c);
-    Lt.planes[0][t] = double2{p.dx, p.bw};
-    Lt.planes[1][t] = double2{p.twcc, p.n_ch};
-    Lt.planes[2][t] = double2{p.ncc, p.s0};
-    Lt.planes[3][t] = double2{p.z, p.bfd};
-    Lt.planes[4][t] = double2{p.sq_s0, p.sq2};
-    Lt.planes[5][t] = double2{p.ck_fac, p.z2};
+    SegRec& r = Lt.recs[(size_t)t];
+    r.p[0] = double2{p.dx, p.bw};
+    r.p[1] = double2{p.twcc, p.n_ch};
+    r.p[2] = double2{p.ncc, p.s0};
+    r.p[3] = double2{p.z, p.bfd};
+    r.p[4] = double2{p.sq_s0, p.sq2};
+    r.p[5] = double2{p.ck_fac, p.z2};
+    r.qcol = qcol;
+    r.qscale = qscale;
+}
+
+static SegRec empty_rec()
+{
+    SegRec r;
+    std::memset(&r, 0, sizeof r);
+    r.qscale = 1.0;
+    return r;
 }
 
 // Schedule and layout of a forest (ALAP levels, level-blocks, tiles).
@@ -372,7 +383,7 @@ static int build_layout(const Forest& f, const std::vector<troute_chparams>& par
         S_int += (long long)hmax * kLanes;
     }
     // one extra slot at the end: the target of segments no reach covers, so
-    // scatter/gather through the segment map never leave the planes
+    // scatter/gather through the segment map never leave the arrays
     Lt.S_int = S_int + 1;
 
     // upstream CSR over internal ids, keeping each reach's upstream order
@@ -399,15 +410,11 @@ static int build_layout(const Forest& f, const std::vector<troute_chparams>& par
     Lt.n_heads = (int)Lt.heads.size();
 
     // parameters in tile order
-    for (auto& p : Lt.planes) p.assign(Lt.S_int, double2{0.0, 0.0});
-    Lt.qcol.assign(Lt.S_int, 0);
-    if (has_scale) Lt.qscale.assign(Lt.S_int, 0.0);
+    Lt.recs.assign((size_t)Lt.S_int, empty_rec());
     for (int s = 0; s < f.S; ++s) {
         const long long t = Lt.seg_map[s];
         if (t < 0) continue;
-        put_params(Lt, t, params[s]);
-        Lt.qcol[t] = qcol_user[s];
-        if (has_scale) Lt.qscale[t] = qscale_user[s];
+        put_params(Lt, t, params[s], qcol_user[s], has_scale ? qscale_user[s] : 1.0);
     }
     return TROUTE_OK;
 }
@@ -483,9 +490,7 @@ static void replicate_layout(const Layout& B, const std::vector<troute_chparams>
         for (int s = 0; s < S; ++s)
             E.seg_map[(size_t)m * S + s] = B.seg_map[s] < 0 ? -1 : B.seg_map[s] + (long long)m * tiles;
     }
-    for (auto& p : E.planes) p.assign((size_t)E.S_int, double2{0.0, 0.0});
-    E.qcol.assign((size_t)E.S_int, 0);
-    E.qscale.assign(q_scale ? (size_t)E.S_int : 0, 0.0);
+    E.recs.assign((size_t)E.S_int, empty_rec());
     for (int m = 0; m < M; ++m)
         for (int s = 0; s < S; ++s) {
             const long long bt = B.seg_map[s];
@@ -497,9 +502,7 @@ static void replicate_layout(const Layout& B, const std::vector<troute_chparams>
                 c.n_ch *= f;
                 c.ncc *= f;
             }
-            put_params(E, t, c);
-            E.qcol[t] = B.qcol[bt];
-            if (q_scale) E.qscale[t] = q_scale[(size_t)m * S + s];
+            put_params(E, t, c, B.recs[(size_t)bt].qcol, q_scale ? q_scale[(size_t)m * S + s] : B.recs[(size_t)bt].qscale);
         }
 }
 
@@ -526,13 +529,9 @@ static int upload_layout(troute_handle* H, Layout& Lt)
         if (m < 0) m = trash;
 
     cudaStream_t st = H->stream;
-    for (int i = 0; i < kParamPlanes; ++i) {
-        if ((rc = upload(H->prm[i], Lt.planes[i], st))) return rc;
-        if ((rc = cuda_check(cudaStreamSynchronize(st), "upload"))) return rc;
-        std::vector<double2>().swap(Lt.planes[i]);
-    }
-    if ((rc = upload(H->qcol, Lt.qcol, st))) return rc;
-    if (!Lt.qscale.empty() && (rc = upload(H->qscale, Lt.qscale, st))) return rc;
+    if ((rc = upload(H->seg, Lt.recs, st))) return rc;
+    if ((rc = cuda_check(cudaStreamSynchronize(st), "upload"))) return rc;
+    std::vector<SegRec>().swap(Lt.recs);
     if ((rc = upload(H->nseg, Lt.nseg, st))) return rc;
     if ((rc = upload(H->tile_off, Lt.tile_off, st))) return rc;
     if ((rc = upload(H->block_level, Lt.block_level, st))) return rc;

@@ -52,6 +52,20 @@ struct SegP {
     double dx, bw, twcc, n_ch, ncc, s0, z, bfd, sq_s0, sq2, ck_fac, z2;
 };
 
+// Everything static a segment solve reads, in one aligned 128-byte record (one
+// L2 line, two DRAM bursts): the six parameter planes' values, the lateral
+// inflow scale (1 when the handle has none: x * 1 is exactly x) and column.
+// The per-lane kernels take (reach, step) items in any order, so a solve's
+// reads are scattered; one record instead of eight separate arrays turns
+// eight sector fetches per solve into one line.
+struct __align__(128) SegRec {
+    double2 p[kParamPlanes];
+    double qscale;
+    int qcol;
+    int pad[5];
+};
+static_assert(sizeof(SegRec) == 128, "one 128-byte line per segment");
+
 // Derived values from the reference's parameter record, :181-183.
 TR_HD inline SegP derive_seg(const troute_chparams& c)
 {
@@ -83,9 +97,7 @@ struct NetDev {
     int n_levels;            // ALAP levels
     int n_reach_int;         // n_blocks * kLanes
     long long n_seg_int;     // padded tile storage
-    const double2* prm[kParamPlanes];  // [n_seg_int] each
-    const int* qcol;         // [n_seg_int] lateral-inflow column of each segment
-    const double* qscale;    // [n_seg_int] or null
+    const SegRec* seg;       // [n_seg_int] parameters, inflow column and scale
     const int* nseg;         // [n_reach_int], -1 for padding lanes
     const long long* tile_off;  // [n_blocks] first segment slot of a block
     const int* block_level;  // [n_blocks]

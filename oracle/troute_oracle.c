@@ -102,6 +102,48 @@ void oracle_pow23_53(double x, double* p23, double* p53)
     *p53 = P53(x);
 }
 
+typedef struct {
+    const double* x;
+    long long b, e;
+    double *p23, *p53;
+    int mode;
+} pow_job;
+
+static void* pow_rows(void* arg)
+{
+    const pow_job* J = (const pow_job*)arg;
+    for (long long i = J->b; i < J->e; ++i) {
+        if (J->mode == 0) {
+            J->p23[i] = pow(J->x[i], 2.0 / 3.0);
+            J->p53[i] = pow(J->x[i], 5.0 / 3.0);
+        } else {
+            cr_pow23_53(J->x[i], &J->p23[i], &J->p53[i]);
+        }
+    }
+    return NULL;
+}
+
+int oracle_pow23_53_n(const double* x, long long n, double* p23, double* p53, int mode, int n_threads)
+{
+    if (n_threads < 1) n_threads = 1;
+    pow_job* J = (pow_job*)calloc((size_t)n_threads, sizeof(pow_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)n_threads, sizeof(pthread_t));
+    if (!J || !th) {
+        free(J), free(th);
+        return 2;
+    }
+    const long long per = (n + n_threads - 1) / n_threads;
+    for (int i = 0; i < n_threads; ++i) {
+        const long long b = i * per, e = (b + per < n) ? b + per : n;
+        J[i] = (pow_job){x, b < n ? b : n, e, p23, p53, mode};
+        if (i > 0) pthread_create(&th[i], NULL, pow_rows, &J[i]);
+    }
+    pow_rows(&J[0]);
+    for (int i = 1; i < n_threads; ++i) pthread_join(th[i], NULL);
+    free(J), free(th);
+    return 0;
+}
+
 /* Channel geometry at depth h: trapezoid plus compound (floodplain) channel.
  * troute_mc_final.cu:30-40 (inlined at :200-205 and :216-221). */
 typedef struct geo {

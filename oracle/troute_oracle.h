@@ -42,6 +42,9 @@ typedef struct oracle_tol {
  * Process-wide; not thread-safe to change while routing. */
 void oracle_set_pow_mode(int mode);
 void oracle_pow23_53(double x, double* p23, double* p53);
+/* The same over an array, mode 0 (C library) or 1 (correctly rounded), on
+ * n_threads POSIX threads; returns 0 (2: out of memory). */
+int oracle_pow23_53_n(const double* x, long long n, double* p23, double* p53, int mode, int n_threads);
 
 /* One segment solve (troute_mc_final.cu:42-139 / :181-248). Returns qdc and
  * writes depth, velocity and the number of secant iterations run. */

@@ -82,6 +82,8 @@ def oracle():
         L.oracle_set_pow_mode.restype = None
         L.oracle_pow23_53.argtypes = [C.c_double, _P, _P]
         L.oracle_pow23_53.restype = None
+        L.oracle_pow23_53_n.argtypes = [_P, C.c_longlong, _P, _P, C.c_int, C.c_int]
+        L.oracle_pow23_53_n.restype = C.c_int
         L.oracle_gen_tree.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int] + [_P] * 4
         L.oracle_gen_tree.restype = C.c_int
         L.oracle_gen_params.argtypes = [C.c_uint64, C.c_int, _P]
@@ -124,6 +126,15 @@ def pow23_53(x: float, mode: int = 0):
     with pow_mode(mode):
         oracle().oracle_pow23_53(float(x), C.byref(a), C.byref(b))
     return a.value, b.value
+
+
+def pow23_53_n(x, mode: int = 1, threads: int = 0):
+    """pow23_53 over an array (all host threads by default) -> (p23, p53)."""
+    x = np.ascontiguousarray(x, np.float64)
+    a, b = np.empty_like(x), np.empty_like(x)
+    if oracle().oracle_pow23_53_n(_ptr(x), x.size, _ptr(a), _ptr(b), int(mode), int(threads or os.cpu_count() or 1)):
+        raise MemoryError("oracle_pow23_53_n")
+    return a, b
 
 
 def ref_available() -> bool:
