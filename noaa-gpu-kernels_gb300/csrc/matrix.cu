@@ -98,13 +98,12 @@ struct MatDev {
     const float* lv;
 };
 
-// Partial of the reference's lane `v` over one matrix row [b, e): entries
-// b + v, b + v + 32, ... accumulated by fused multiply-add from 0.
-__device__ __forceinline__ float lane_partial(const int* __restrict__ col, const float* __restrict__ val,
-                                              const float* __restrict__ vec, int b, int e, int v)
+// Continues the reference's lane `v` over one matrix row [b, e) from entry
+// k0 on: entries k0, k0 + 32, ... accumulated by fused multiply-add onto s.
+__device__ __forceinline__ float lane_tail(const int* __restrict__ col, const float* __restrict__ val,
+                                           const float* __restrict__ vec, int k0, int e, float s)
 {
-    float s = 0.0f;
-    for (int k = b + v; k < e; k += 32) s = __fmaf_rn(__ldg(val + k), __ldg(vec + __ldg(col + k)), s);
+    for (int k = k0; k < e; k += 32) s = __fmaf_rn(__ldg(val + k), __ldg(vec + __ldg(col + k)), s);
     return s;
 }
 
@@ -117,11 +116,37 @@ __global__ void __launch_bounds__(kMatThreads) mat_step_kernel(MatDev m, const f
     if (row < m.R) {
         const int qb = __ldg(m.qp + row), qe = __ldg(m.qp + row + 1);
         const int lb = __ldg(m.lp + row), le = __ldg(m.lp + row + 1);
+        // the first entry of each of the reference's lanes p, p+8, p+16, p+24
+        // (rows of up to 32 entries have no other): every column and value
+        // load is issued before any gather, and every gather before any sum,
+        // so a row costs two memory round trips instead of a chain of them
+        int cq[4], cl[4];
+        float vq[4], vl[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int kq = qb + p + kLanesPerRow * j, kl = lb + p + kLanesPerRow * j;
+            cq[j] = kq < qe ? __ldg(m.qc + kq) : 0;
+            vq[j] = kq < qe ? __ldg(m.qv + kq) : 0.0f;
+            cl[j] = kl < le ? __ldg(m.lc + kl) : 0;
+            vl[j] = kl < le ? __ldg(m.lv + kl) : 0.0f;
+        }
+        float xq[4], xl[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int kq = qb + p + kLanesPerRow * j, kl = lb + p + kLanesPerRow * j;
+            xq[j] = kq < qe ? __ldg(x + cq[j]) : 0.0f;
+            xl[j] = kl < le ? __ldg(ql + cl[j]) : 0.0f;
+        }
         float s[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int v = p + kLanesPerRow * j;   // the reference's lane
-            s[j] = __fadd_rn(lane_partial(m.qc, m.qv, x, qb, qe, v), lane_partial(m.lc, m.lv, ql, lb, le, v));
+            const int kq = qb + p + kLanesPerRow * j, kl = lb + p + kLanesPerRow * j;
+            // fma(v, x, 0) where the lane holds an entry, 0 where it holds none
+            float sq = kq < qe ? __fmaf_rn(vq[j], xq[j], 0.0f) : 0.0f;
+            float sl = kl < le ? __fmaf_rn(vl[j], xl[j], 0.0f) : 0.0f;
+            if (kq + 32 < qe) sq = lane_tail(m.qc, m.qv, x, kq + 32, qe, sq);
+            if (kl + 32 < le) sl = lane_tail(m.lc, m.lv, ql, kl + 32, le, sl);
+            s[j] = __fadd_rn(sq, sl);
         }
         // shuffle-down levels 16 and 8 of the reference's tree, in registers:
         // lane v + 16 onto v, then (v + 8) onto v
