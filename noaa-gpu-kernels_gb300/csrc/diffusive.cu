@@ -36,19 +36,32 @@ struct DiffTiles {
     float qp[kDWarps][kDW][kTileLd];
 };
 
-// Loads nodes [n0, n0 + cnt) of rows r0..r0+31 of `src` into tile[row][k0 + j]
-// (coalesced along the row; nodes outside [0, max_nodes) or rows past n_reaches
-// are left untouched).
+// Loads nodes [n0, n0 + cnt) (cnt <= 64) of rows r0..r0+31 of `src` into
+// tile[row][k0 + j] (coalesced along the row; nodes outside [0, max_nodes) or
+// rows past n_reaches are left untouched). Eight rows at a time: their loads
+// are all issued before any is stored, so a tile costs four memory round
+// trips, not one per row.
 __device__ __forceinline__ void load_tile(float (*tile)[kTileLd], const float* __restrict__ src, int r0, int n_reaches,
                                           int max_nodes, int n0, int cnt, int k0, int lane)
 {
-    for (int row = 0; row < kDW; ++row) {
-        const int r = r0 + row;
-        if (r >= n_reaches) break;
-        const float* p = src + (size_t)r * (size_t)max_nodes;
-        for (int j = lane; j < cnt; j += kDW) {
-            const int node = n0 + j;
-            if (node >= 0 && node < max_nodes) tile[row][k0 + j] = __ldg(p + node);
+    const int na = n0 + lane, nb = n0 + lane + kDW;
+    const bool ok_a = lane < cnt && na >= 0 && na < max_nodes;
+    const bool ok_b = lane + kDW < cnt && nb >= 0 && nb < max_nodes;
+    for (int row0 = 0; row0 < kDW; row0 += 8) {
+        float va[8], vb[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int r = r0 + row0 + q;
+            const bool in = r < n_reaches;
+            va[q] = (in && ok_a) ? __ldg(src + (size_t)r * (size_t)max_nodes + na) : 0.0f;
+            vb[q] = (in && ok_b) ? __ldg(src + (size_t)r * (size_t)max_nodes + nb) : 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            if (r0 + row0 + q < n_reaches) {
+                if (ok_a) tile[row0 + q][k0 + lane] = va[q];
+                if (ok_b) tile[row0 + q][k0 + lane + kDW] = vb[q];
+            }
         }
     }
 }
@@ -132,10 +145,28 @@ __global__ void __launch_bounds__(kDW * kDWarps) diffusive_kernel(const troute_d
             T.qp[w][lane][nc - 1 - i0] = next;
         }
         if (live) {
+            // the tile's elimination coefficients first, eight nodes' loads in
+            // flight at a time, into the lane's rows of the dx / diffusivity
+            // tiles (free once the forward sweep is done); then the
+            // recurrence reads them from shared memory
+            for (int k0 = 0; k0 < kDW; k0 += 8) {
+                float ev[8], fv[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int i = i0 + k0 + q;
+                    ev[q] = i < nc - 1 ? se[(size_t)i * n_reaches + r] : 0.0f;
+                    fv[q] = i < nc - 1 ? sf[(size_t)i * n_reaches + r] : 0.0f;
+                }
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    T.dx[w][lane][k0 + q] = ev[q];
+                    T.diff[w][lane][k0 + q] = fv[q];
+                }
+            }
             for (int k = kDW - 1; k >= 0; --k) {
                 const int i = i0 + k;
                 if (i >= nc - 1) continue;
-                next = se[(size_t)i * n_reaches + r] * next + sf[(size_t)i * n_reaches + r];
+                next = T.dx[w][lane][k] * next + T.diff[w][lane][k];
                 T.qp[w][lane][k] = next;
             }
         }
