@@ -800,7 +800,7 @@ def run_ours(args, dist: Dist):
                              f"segment parameters {S * 96 / 1e9:.2f} GB read per bench step",
                        "parallelism": par},
             "roofline": roofline, "critical_path": crit, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": 4 * args.steps, "parity": parity,
+            "gpu_launches": (5 if model else 4) * args.steps, "parity": parity,
             "max_rel_err": None if parity is None else parity["max_rel_err"],
             "solver": {"iterations_per_solve": it / max(1, stats["solves"]), "retries": stats["retries"],
                        "early_exits": stats["early_exits"], "warm_used": stats["warm_used"],

@@ -57,9 +57,9 @@ __device__ __forceinline__ SegP staged_seg(const double2* slot)
     p.z = e.x; p.bfd = e.y; p.sq_s0 = f.x; p.sq2 = f.y; p.ck_fac = g.x; p.z2 = g.y;
     return p;
 }
-// Warm-start phase of a solve: plain bracket, waiting for the learned depth
-// (set by the kernel before the next pass), or bracketing the learned depth.
-enum : int { W_PLAIN = 0, W_PENDING = 1, W_ACTIVE = 2 };
+// Warm-start phase of a solve: the plain bracket, or bracketing the learned
+// depth (read from the launch's prediction plane when the solve begins).
+enum : int { W_PLAIN = 0, W_ACTIVE = 2 };
 
 // Everything a lane carries for one (reach, step) and the segment it solves.
 struct Lane {
@@ -129,7 +129,23 @@ __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const 
         plain_bracket(L, run.tol);
         L.total = 0;
         L.retried = 0;
-        L.warm = run.warm ? W_PENDING : W_PLAIN;
+        L.warm = W_PLAIN;
+        if (run.warm) {
+            // the learned starting depth of this solve, predicted before the launch:
+            // the bracket [p (1 - delta), p (1 + delta)] around a positive normal
+            // float p below 1e4 m (0x461c4000), else the plain bracket
+            const float prf = __ldcg(run.start_pred + (size_t)L.tau * (size_t)net.n_seg_int + L.s);
+            const unsigned pb = __float_as_uint(prf);
+            if (pb >= 0x00800000u && pb < 0x461c4000u) {
+                const double pr = __longlong_as_double(((long long)((pb >> 23) + 896) << 52) |
+                                                       ((long long)(pb & 0x7fffff) << 29));  // exact widening
+                L.h = pr * run.warm_hi;
+                L.h_0 = pr * run.warm_lo;
+                L.warm = W_ACTIVE;
+                ls.warm_used++;
+                if (run.start_hist) __stcg(run.start_hist + (size_t)L.tau * (size_t)net.n_seg_int + L.s, pr);
+            }
+        }
         return true;
     }
     return false;
@@ -142,7 +158,7 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
     const Tol& tol = run.tol;
     const double dt = run.dt;
     const double dt2 = run.dt_half;  // dt / 2 (exact), formed on the host
-    if (L.mode == L_SOLVE && L.warm != W_PENDING) {
+    if (L.mode == L_SOLVE) {
         // the segment's parameters, staged in shared memory when the solve began
         const SegP p = staged_seg(slot);
         const double x = L.need0 ? L.h_0 : L.h;  // >= +0

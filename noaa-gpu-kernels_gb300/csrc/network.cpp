@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <array>
 #include <cstdarg>
 #include <cstdio>
@@ -201,6 +202,7 @@ struct troute_handle {
     double warm_delta = 0.05;
     DBuf<float> pairs;        // [n_ts][S_int][9]
     DBuf<double> start_hist;  // [n_ts][S_int]
+    DBuf<float> pred;         // [chunk][S_int] learned starting depths of a warm-started launch
     int pairs_ts = 0, start_ts = 0;
 
     cudaStream_t stream = nullptr;
@@ -246,7 +248,7 @@ struct troute_handle {
         qlat_buf.release(); hist.release(); tile_off.release(); seg_map_d.release();
         reach_map_d.release(); wave_ptr.release(); wave_ptr_tail.release(); ticket.release(); stats.release();
         rq_ctr.release(); df_cnt.release(); df_rq.release(); df_heads.release(); df_rh.release();
-        pairs.release(); start_hist.release();
+        pairs.release(); start_hist.release(); pred.release();
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -318,6 +320,7 @@ static SegRec empty_rec()
     SegRec r;
     std::memset(&r, 0, sizeof r);
     r.qscale = 1.0;
+    r.reach = -1;
     return r;
 }
 
@@ -416,6 +419,12 @@ static int build_layout(const Forest& f, const std::vector<troute_chparams>& par
         if (t < 0) continue;
         put_params(Lt, t, params[s], qcol_user[s], has_scale ? qscale_user[s] : 1.0);
     }
+    for (int r = 0; r < R; ++r)
+        for (int i = 0; i < f.seg_len[r]; ++i) {
+            const long long t = Lt.seg_map[f.seg_start[r] + i];
+            Lt.recs[(size_t)t].reach = (int)Lt.reach_map[r];
+            Lt.recs[(size_t)t].pos = i;
+        }
     return TROUTE_OK;
 }
 
@@ -503,6 +512,8 @@ static void replicate_layout(const Layout& B, const std::vector<troute_chparams>
                 c.ncc *= f;
             }
             put_params(E, t, c, B.recs[(size_t)bt].qcol, q_scale ? q_scale[(size_t)m * S + s] : B.recs[(size_t)bt].qscale);
+            E.recs[(size_t)t].reach = B.recs[(size_t)bt].reach >= 0 ? new_reach(m, B.recs[(size_t)bt].reach) : -1;
+            E.recs[(size_t)t].pos = B.recs[(size_t)bt].pos;
         }
 }
 
@@ -825,13 +836,19 @@ struct RunPlan {
     int chunk = 0, n_full = 0, rem = 0;
 };
 
+constexpr int kWarmLaunchSteps = 32;
+
 static int plan_run(troute_handle* H, int n_ts, RunPlan* P)
 {
     int chunk = n_ts;
     if (H->cfg.max_chunk_steps > 0) chunk = std::min(chunk, H->cfg.max_chunk_steps);
+    // warm-started launches predict every solve's starting depth from the state
+    // at the launch's start: at most kWarmLaunchSteps steps per launch keep it recent
+    if (H->cfg.warm_start) chunk = std::min(chunk, kWarmLaunchSteps);
     if (H->mapping == 3) {
         const double per_step = (double)std::max(1, H->R_int) * (sizeof(int) + sizeof(double)) +
-                                (double)std::max(1, H->R_real) * sizeof(int2);
+                                (double)std::max(1, H->R_real) * sizeof(int2) +
+                                (H->cfg.warm_start ? (double)H->S_int * sizeof(float) : 0.0);
         if (H->chunk_budget_bytes == 0) {
             size_t fr = 0, tot = 0;
             if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) fr = (size_t)8 << 30;
@@ -874,6 +891,7 @@ static int enqueue_chunk(troute_handle* H, const double* qlat_dev, int n_ts, con
     run.warm_delta = H->warm_delta;
     run.warm_hi = 1.0 + H->warm_delta;
     run.warm_lo = 1.0 - H->warm_delta;
+    run.start_pred = nullptr;
     if ((rc = cuda_check(cudaMemsetAsync(H->ticket.p, 0, sizeof(unsigned long long), st), "memset"))) return rc;
     if (H->mapping == 3) {
         DataflowDev df;
@@ -887,7 +905,17 @@ static int enqueue_chunk(troute_handle* H, const double* qlat_dev, int n_ts, con
         df.n_heads = H->n_heads;
         df.continue_items = H->cfg.schedule_flags & 1;
         df.n_items = (unsigned long long)H->R_real * (unsigned long long)n_ts;
-        rc = launch_route_dataflow(H->net(), run, df, H->warm_model, H->grid, st);
+        if (run.warm) {
+            // the launch's learned starting depths: one tcgen05 GEMM over every
+            // (segment slot, step) from the state at the launch's start
+            if (!warm_ready(H->warm_model))
+                return set_error(TROUTE_ESTATE, "cfg.warm_start is set but no trained model is attached");
+            int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(H->stats.p) + offsetof(DevStats, error));
+            if ((rc = launch_warm_plane(H->warm_model, H->net(), run, n_ts, H->pred.p, err, st)))
+                return rc;
+            run.start_pred = H->pred.p;
+        }
+        rc = launch_route_dataflow(H->net(), run, df, H->grid, st);
     } else if (H->mapping == 2) {
         rc = launch_route_pool(H->net(), run, H->grid, H->threads, st);
     } else {
@@ -966,6 +994,7 @@ static int prepare_run(troute_handle* H, int n_ts, RunPlan* P)
         if ((rc = H->start_hist.alloc((size_t)n_ts * H->S_int))) return rc;
         H->start_ts = n_ts;
     }
+    if (H->cfg.warm_start && (rc = H->pred.alloc((size_t)P->chunk * H->S_int))) return rc;
     if (H->mapping == 3) {
         const size_t R = (size_t)std::max(1, H->R_int);
         const size_t T = (size_t)P->chunk;

@@ -27,7 +27,6 @@
 // (wavefront_mc.cu:525-531), and the solve is lane_solver.cuh's, i.e. the
 // reference's arithmetic.
 #include "lane_solver.cuh"
-#include "warm.cuh"
 
 namespace tr {
 
@@ -103,68 +102,21 @@ __device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base,
     L.mode = begin_segment(L, net, run, ls, hist_s, slot) ? L_SOLVE : L_DONE;
 }
 
-// Learned starting depth for every lane of the warp whose solve waits for one
-// (W_PENDING): one tensor-core MLP evaluation for the whole warp, then the
-// bracket [p (1 - delta), p (1 + delta)] around the prediction p. A prediction
-// that is not a positive finite depth below 1e4 m leaves the plain bracket.
-__device__ __forceinline__ void warm_predict_lanes(Lane& L, WarmSmem& s, const WarmDev& m, const NetDev& net,
-                                                   const RunDev& run, LocalStats& ls, const double2* slot)
-{
-    const bool pend = (L.mode == L_SOLVE && L.warm == W_PENDING);
-    if (!__any_sync(0xffffffffu, pend)) return;
-    float f[kWIn];
-    if (pend) {
-        // features on the FP32 / integer pipes: truncating double -> float
-        f[0] = warm_feature(pos_to_float(L.qup), true, m.mu[0], m.inv_sd[0]);
-        f[1] = warm_feature(pos_to_float(L.quc), true, m.mu[1], m.inv_sd[1]);
-        f[2] = warm_feature(pos_to_float(L.qdp), true, m.mu[2], m.inv_sd[2]);
-        f[3] = warm_feature(pos_to_float(L.ql), true, m.mu[3], m.inv_sd[3]);
-        const double2 p0 = slot[0], p1 = slot[kSegSmemStride], p2 = slot[2 * kSegSmemStride];
-        f[4] = warm_feature(pos_to_float(p0.x), false, m.mu[4], m.inv_sd[4]);   // dx
-        f[5] = warm_feature(pos_to_float(p2.y), false, m.mu[5], m.inv_sd[5]);   // s0
-        f[6] = warm_feature(pos_to_float(p1.y), false, m.mu[6], m.inv_sd[6]);   // n
-        f[7] = warm_feature(pos_to_float(p0.y), false, m.mu[7], m.inv_sd[7]);   // bw
-    } else {
-        for (int k = 0; k < kWIn; ++k) f[k] = 0.0f;
-    }
-    const float y = warm_mlp_warp(s, f, pend, m.b3);
-    if (pend) {
-        const float prf = __expf(y * m.sd_y + m.mu_y);
-        const unsigned pb = __float_as_uint(prf);
-        // a normal positive float below 1e4 m (0x461c4000), else the plain bracket
-        if (pb >= 0x00800000u && pb < 0x461c4000u) {
-            const double pr = widen_pos(prf);
-            L.h = pr * run.warm_hi;   // 1 + delta
-            L.h_0 = pr * run.warm_lo; // 1 - delta
-            L.warm = W_ACTIVE;
-            ls.warm_used++;
-            if (run.start_hist) __stcg(run.start_hist + (size_t)L.tau * (size_t)net.n_seg_int + L.s, pr);
-        } else {
-            L.warm = W_PLAIN;
-        }
-    }
-}
-
-// Resident blocks per SM the register allocation is sized for (plain and
-// warm-started kernels).
+// Resident blocks per SM the register allocation is sized for.
 #ifndef TROUTE_DF_MINB
 #define TROUTE_DF_MINB 1
 #endif
-#ifndef TROUTE_DFW_MINB
-#define TROUTE_DFW_MINB 3
-#endif
 
-template <bool WARM>
-__global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
-    route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df, WarmDev wm)
+// Warm-started runs read each solve's learned starting depth from the
+// prediction plane the launch's GEMM filled (warm_gemm.cu) when the solve
+// begins (lane_solver.cuh, begin_segment): the same kernel serves plain and
+// warm-started runs.
+__global__ void __launch_bounds__(128, TROUTE_DF_MINB) route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df)
 {
     __shared__ unsigned int hist_s[16];
     __shared__ double2 seg_sm[kParamPlanes * kSegSmemStride];
     double2* const seg_slot = seg_sm + threadIdx.x;
-    extern __shared__ __align__(16) unsigned char dyn_smem[];
-    WarmSmem& wsm = *reinterpret_cast<WarmSmem*>(dyn_smem);
     if (threadIdx.x < 16) hist_s[threadIdx.x] = 0;
-    if constexpr (WARM) warm_stage(wsm, wm);
     __syncthreads();
     LocalStats ls = {0, 0, 0, 0, 0, 0};
     const int lane = threadIdx.x & 31;
@@ -290,9 +242,6 @@ __global__ void __launch_bounds__(128, WARM ? TROUTE_DFW_MINB : TROUTE_DF_MINB)
             }
         }
 
-        // ---- learned starting depths for solves that just began ----
-        if constexpr (WARM) warm_predict_lanes(L, wsm, wm, net, run, ls, seg_slot);
-
         // ---- one depth evaluation per solving lane ----
         if (__any_sync(kFullMask, L.mode >= L_SOLVE)) {
             n_solve++;
@@ -408,10 +357,9 @@ __global__ void dataflow_init_kernel(NetDev net, RunDev run, DataflowDev df)
     }
 }
 
-int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, const troute_warm* warm,
-                          int grid, void* stream)
+int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, int grid, void* stream)
 {
-    if (run.warm && !warm_ready(warm)) return set_error(TROUTE_ESTATE, "warm start requested without a trained model");
+    if (run.warm && !run.start_pred) return set_error(TROUTE_ESTATE, "warm start requested without a prediction plane");
     if (df.n_items == 0) return TROUTE_OK;
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e;
@@ -427,23 +375,15 @@ int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDe
     if (ig > 4096) ig = 4096;
     if (ig < 1) ig = 1;
     dataflow_init_kernel<<<ig, 256, 0, st>>>(net, run, df);
-    if (run.warm) {
-        route_dataflow_kernel<true>
-            <<<grid, 128, sizeof(WarmSmem), st>>>(net, run, df, warm_device_view(warm, run.warm_delta, run.warm_k));
-    } else {
-        route_dataflow_kernel<false><<<grid, 128, 0, st>>>(net, run, df, WarmDev{});
-    }
+    route_dataflow_kernel<<<grid, 128, 0, st>>>(net, run, df);
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(TROUTE_ECUDA, "route_dataflow_kernel launch: %s", cudaGetErrorString(e));
     return TROUTE_OK;
 }
 
-int route_dataflow_occupancy(int* blocks_per_sm, bool warm)
+int route_dataflow_occupancy(int* blocks_per_sm, bool)
 {
-    const cudaError_t e =
-        warm ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, route_dataflow_kernel<true>, 128,
-                                                             sizeof(WarmSmem))
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, route_dataflow_kernel<false>, 128, 0);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, route_dataflow_kernel, 128, 0);
     if (e != cudaSuccess) return set_error(TROUTE_ECUDA, "occupancy query: %s", cudaGetErrorString(e));
     return TROUTE_OK;
 }

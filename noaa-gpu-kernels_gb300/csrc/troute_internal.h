@@ -62,7 +62,9 @@ struct __align__(128) SegRec {
     double2 p[kParamPlanes];
     double qscale;
     int qcol;
-    int pad[5];
+    int reach;   // internal reach of the slot (-1: a slot no segment uses)
+    int pos;     // position of the segment in its reach
+    int pad[3];
 };
 static_assert(sizeof(SegRec) == 128, "one 128-byte line per segment");
 
@@ -132,6 +134,7 @@ struct RunDev {
     float* pairs;            // optional [n_ts][n_seg_int][9] training pairs (qup quc qdp ql dx s0 n bw depth)
     double* start_hist;      // optional [n_ts][n_seg_int] learned starting depth of each solve (0: plain)
     int warm;                // 1: solves start from the learned depth (dataflow kernel only)
+    const float* start_pred; // [n_ts][n_seg_int] learned starting depth of every solve (warm runs)
     int warm_k;              // passes of the warm phase before the plain fallback
     double warm_delta;       // relative half-width of the warm bracket
     double warm_hi, warm_lo; // 1 + warm_delta, 1 - warm_delta
@@ -161,8 +164,16 @@ int launch_route(const NetDev& net, const RunDev& run, int grid, int threads, vo
 int route_occupancy(int threads, int* blocks_per_sm);
 int launch_route_pool(const NetDev& net, const RunDev& run, int grid, int threads, void* stream);
 int route_pool_occupancy(int* blocks_per_sm);
-int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, const troute_warm* warm,
-                          int grid, void* stream);
+int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDev& df, int grid, void* stream);
+// Learned starting depths of a routing launch of T steps (warm_gemm.cu): the
+// MLP as one tcgen05 GEMM over every (segment slot, step), features from the
+// state at the launch's start; plane [T][n_seg_int]. A stalled wait sets
+// *error to TROUTE_ETIMEOUT.
+int launch_warm_plane(const troute_warm* w, const NetDev& net, const RunDev& run, int T, float* plane, int* error,
+                      void* stream);
+// The same GEMM for raw inputs [n][8] (device arrays).
+int launch_warm_gemm_raw(const troute_warm* w, const float* raw, long long n, double* depth, int* error,
+                         void* stream);
 // Learned warm start (warm.cu): whether a model has weights on the device, and
 // the compaction of the dense per-solve pair records [n_rows][9] (rows with a
 // positive depth) into `out`, in row order; synchronous on `stream`.

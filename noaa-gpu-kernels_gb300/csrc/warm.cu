@@ -618,6 +618,29 @@ extern "C" int troute_warm_grad(troute_warm* w, const float* pairs_host, int n, 
     return rc;
 }
 
+extern "C" int troute_warm_predict_gemm(troute_warm* w, const float* raw_host, int n, double* depth_out)
+{
+    if (!w || !raw_host || n < 1 || !depth_out) return set_error(TROUTE_EINVAL, "bad arguments");
+    if (!w->trained) return set_error(TROUTE_ESTATE, "model has no weights (train or set them first)");
+    float* d_raw = nullptr;
+    double* d_out = nullptr;
+    int* d_err = nullptr;
+    int rc = warm_cuda(cudaMalloc(&d_raw, (size_t)n * kWIn * sizeof(float)), "cudaMalloc");
+    if (!rc) rc = warm_cuda(cudaMalloc(&d_out, (size_t)n * sizeof(double)), "cudaMalloc");
+    if (!rc) rc = warm_cuda(cudaMalloc(&d_err, sizeof(int)), "cudaMalloc");
+    if (!rc) rc = warm_cuda(cudaMemset(d_err, 0, sizeof(int)), "memset");
+    if (!rc) rc = warm_cuda(cudaMemcpy(d_raw, raw_host, (size_t)n * kWIn * sizeof(float), cudaMemcpyHostToDevice), "H2D");
+    if (!rc) rc = launch_warm_gemm_raw(w, d_raw, n, d_out, d_err, nullptr);
+    int err = 0;
+    if (!rc) rc = warm_cuda(cudaMemcpy(depth_out, d_out, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
+    if (!rc) rc = warm_cuda(cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+    cudaFree(d_raw);
+    cudaFree(d_out);
+    cudaFree(d_err);
+    if (!rc && err) rc = set_error(err, "warm GEMM: a tensor-core completion wait ran out");
+    return rc;
+}
+
 extern "C" int troute_warm_predict(troute_warm* w, const float* raw_host, int n, double* depth_out)
 {
     if (!w || !raw_host || n < 1 || !depth_out) return set_error(TROUTE_EINVAL, "bad arguments");

@@ -154,6 +154,7 @@ _SIGS = {
     "troute_warm_fit": ([_P, _P, C.c_longlong, _I, _I, C.c_float, C.c_float, _U64, _P], _I),
     "troute_warm_grad": ([_P, _P, _I, _P, _P], _I),
     "troute_warm_predict": ([_P, _P, _I, _P], _I),
+    "troute_warm_predict_gemm": ([_P, _P, _I, _P], _I),
     "troute_set_warm_start": ([_P, _P, _D], _I),
     "troute_get_pairs": ([_P, _P, C.c_longlong, _P], _I),
     "troute_get_start_history": ([_P, _P, _I], _I),
@@ -869,6 +870,14 @@ class WarmModel:
         x = np.ascontiguousarray(inputs, np.float32).reshape(-1, 8)
         out = np.zeros(x.shape[0])
         _check(lib().troute_warm_predict(self._h, _ptr(x), x.shape[0], _ptr(out)))
+        return out
+
+    def predict_gemm(self, inputs) -> np.ndarray:
+        """The same through the tcgen05 GEMM that fills a warm-started launch's
+        starting depths."""
+        x = np.ascontiguousarray(inputs, np.float32).reshape(-1, 8)
+        out = np.zeros(x.shape[0])
+        _check(lib().troute_warm_predict_gemm(self._h, _ptr(x), x.shape[0], _ptr(out)))
         return out
 
 

@@ -24,8 +24,8 @@ INCLUDE = os.path.join(os.path.dirname(PKG_ROOT), "include")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "route_pool.cu", "route_dataflow.cu", "noalloc.cu", "warm.cu", "linear.cu", "diffusive.cu",
-              "matrix.cu"]
+CU_SOURCES = ["kernels.cu", "route_pool.cu", "route_dataflow.cu", "noalloc.cu", "warm.cu", "warm_gemm.cu", "linear.cu",
+              "diffusive.cu", "matrix.cu"]
 CPP_SOURCES = ["network.cpp", "capi.cpp", "gen.cpp", "netfile.cpp", "forcing.cpp"]
 
 

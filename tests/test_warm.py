@@ -174,6 +174,38 @@ def test_tensor_core_inference_matches_bf16_emulation():
     assert np.median(np.abs(np.log(pred / ref32))) < 0.02 * sd_y
 
 
+def test_tcgen05_gemm_inference_matches_bf16_emulation():
+    """The tcgen05 GEMM that fills warm-started launches' starting depths
+    (troute_warm_predict_gemm): BF16 features and weights, FP32 accumulation
+    in tensor memory, SiLU and the last layer in FP32. 100,003 rows: a partial
+    last 128-row tile and more tiles than resident CTAs. Checked against a
+    torch emulation of that arithmetic, the FP32 network and the per-warp
+    mma.sync path."""
+    pairs = synthetic_pairs(100_003, 16)
+    st = random_state(pairs, 17)
+    m = T.WarmModel(0)
+    m.set_state(st)
+    pred = m.predict_gemm(pairs[:, :8])
+    assert np.isfinite(pred).all() and (pred > 0).all()
+    W1, b1, W2, b2, w3, b3, mu, sd, mu_y, sd_y = unpack(st)
+    x = torch.tensor(features(pairs, mu, sd))
+    silu = lambda z: z / (1 + torch.exp(-z))
+    a1 = bf16(silu(bf16(x) @ bf16(W1).T + torch.tensor(b1, dtype=torch.float32)))
+    y = silu(a1 @ bf16(W2).T + torch.tensor(b2, dtype=torch.float32)) @ bf16(w3) + np.float32(b3)
+    emu = np.exp(y.numpy().astype(np.float64) * sd_y + mu_y)
+    r = np.abs(pred / emu - 1)
+    print(f"\ntcgen05 GEMM inference vs emulation: median {np.median(r):.2e}, max {r.max():.2e}")
+    # tanh.approx in the kernel's SiLU against the exact one, rounded to bf16
+    assert np.median(r) < 1e-2 and r.max() < 8e-2
+    f1 = silu(x @ torch.tensor(W1, dtype=torch.float32).T + torch.tensor(b1, dtype=torch.float32))
+    f2 = silu(f1 @ torch.tensor(W2, dtype=torch.float32).T + torch.tensor(b2, dtype=torch.float32))
+    ref32 = np.exp((f2 @ torch.tensor(w3, dtype=torch.float32) + np.float32(b3)).numpy().astype(np.float64) * sd_y
+                   + mu_y)
+    assert np.median(np.abs(np.log(pred / ref32))) < 0.02 * sd_y
+    per_warp = m.predict(pairs[:, :8])
+    assert np.median(np.abs(pred / per_warp - 1)) < 2e-2
+
+
 def record_pairs(net_name, seed, n_ts):
     """Pairs of a plain tight-tolerance run, on the device (torch buffer)."""
     c = synth.network(net_name, seed=seed, n_ts=n_ts)
