@@ -836,15 +836,10 @@ struct RunPlan {
     int chunk = 0, n_full = 0, rem = 0;
 };
 
-constexpr int kWarmLaunchSteps = 32;
-
 static int plan_run(troute_handle* H, int n_ts, RunPlan* P)
 {
     int chunk = n_ts;
     if (H->cfg.max_chunk_steps > 0) chunk = std::min(chunk, H->cfg.max_chunk_steps);
-    // warm-started launches predict every solve's starting depth from the state
-    // at the launch's start: at most kWarmLaunchSteps steps per launch keep it recent
-    if (H->cfg.warm_start) chunk = std::min(chunk, kWarmLaunchSteps);
     if (H->mapping == 3) {
         const double per_step = (double)std::max(1, H->R_int) * (sizeof(int) + sizeof(double)) +
                                 (double)std::max(1, H->R_real) * sizeof(int2) +
