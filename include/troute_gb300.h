@@ -295,14 +295,12 @@ int troute_warm_fit(troute_warm* model, const float* pairs_device, long long n_p
  * standardisation (the training kernel's forward and backward pass):
  * grad_out [TROUTE_WARM_NPARAMS], loss_out = mean (err^2)/2. */
 int troute_warm_grad(troute_warm* model, const float* pairs_host, int n, float* grad_out, double* loss_out);
-/* Predicted depths for n host input rows [n][8] (the tensor-core path). */
+/* Predicted depths for n host input rows [n][8], through the GEMM that
+ * warm-started runs use: the MLP as BF16 tcgen05 matrix multiplies (M = 128
+ * rows per tile, FP32 accumulators in tensor memory); before each
+ * warm-started routing launch this GEMM fills the starting depth of every
+ * (segment, step) of the launch from the state at the launch's start. */
 int troute_warm_predict(troute_warm* model, const float* inputs_host, int n, double* depth_out);
-/* The same predictions through the GEMM that warm-started runs use: the MLP
- * as BF16 tcgen05 matrix multiplies (M = 128 rows per tile, FP32 accumulators
- * in tensor memory); before each warm-started routing launch this GEMM fills
- * the starting depth of every (segment, step) of the launch from the state at
- * the launch's start. No counterpart in the reference. */
-int troute_warm_predict_gemm(troute_warm* model, const float* inputs_host, int n, double* depth_out);
 
 /* Attaches a trained model to a handle (NULL detaches); runs with
  * cfg.warm_start = 1 use it. The model must outlive the handle's runs; a

@@ -234,23 +234,6 @@ __global__ void warm_adamw_kernel(float* __restrict__ prm, const float* __restri
     }
 }
 
-// Predicts depths for raw inputs with the tensor-core path the solver uses.
-__global__ void __launch_bounds__(128) warm_predict_kernel(WarmDev m, const float* __restrict__ raw, int n,
-                                                           double* __restrict__ depth)
-{
-    __shared__ WarmSmem s;
-    warm_stage(s, m);
-    __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float f[kWIn];
-    for (int k = 0; k < kWIn; ++k) {
-        const float v = (i < n) ? raw[(size_t)i * kWIn + k] : 1.0f;
-        f[k] = warm_feature(v, k < 4, m.mu[k], m.inv_sd[k]);
-    }
-    const float yh = warm_mlp_warp(s, f, i < n, m.b3);
-    if (i < n) depth[i] = (double)__expf(yh * m.sd_y + m.mu_y);
-}
-
 // Pair compaction: valid rows (depth > 0) per 1024-row block, then their
 // scatter to the block's offset in row order.
 constexpr int kCompactRows = 1024;
@@ -618,7 +601,7 @@ extern "C" int troute_warm_grad(troute_warm* w, const float* pairs_host, int n, 
     return rc;
 }
 
-extern "C" int troute_warm_predict_gemm(troute_warm* w, const float* raw_host, int n, double* depth_out)
+extern "C" int troute_warm_predict(troute_warm* w, const float* raw_host, int n, double* depth_out)
 {
     if (!w || !raw_host || n < 1 || !depth_out) return set_error(TROUTE_EINVAL, "bad arguments");
     if (!w->trained) return set_error(TROUTE_ESTATE, "model has no weights (train or set them first)");
@@ -638,27 +621,5 @@ extern "C" int troute_warm_predict_gemm(troute_warm* w, const float* raw_host, i
     cudaFree(d_out);
     cudaFree(d_err);
     if (!rc && err) rc = set_error(err, "warm GEMM: a tensor-core completion wait ran out");
-    return rc;
-}
-
-extern "C" int troute_warm_predict(troute_warm* w, const float* raw_host, int n, double* depth_out)
-{
-    if (!w || !raw_host || n < 1 || !depth_out) return set_error(TROUTE_EINVAL, "bad arguments");
-    if (!w->trained) return set_error(TROUTE_ESTATE, "model has no weights (train or set them first)");
-    float* d_raw = nullptr;
-    double* d_out = nullptr;
-    int rc;
-    if ((rc = warm_cuda(cudaMalloc(&d_raw, (size_t)n * kWIn * sizeof(float)), "cudaMalloc"))) return rc;
-    if ((rc = warm_cuda(cudaMalloc(&d_out, (size_t)n * sizeof(double)), "cudaMalloc"))) {
-        cudaFree(d_raw);
-        return rc;
-    }
-    rc = warm_cuda(cudaMemcpy(d_raw, raw_host, (size_t)n * kWIn * sizeof(float), cudaMemcpyHostToDevice), "H2D");
-    if (!rc) {
-        warm_predict_kernel<<<(n + 127) / 128, 128>>>(warm_device_view(w, 0.0, 0), d_raw, n, d_out);
-        rc = warm_cuda(cudaMemcpy(depth_out, d_out, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost), "D2H");
-    }
-    cudaFree(d_raw);
-    cudaFree(d_out);
     return rc;
 }

@@ -154,7 +154,6 @@ _SIGS = {
     "troute_warm_fit": ([_P, _P, C.c_longlong, _I, _I, C.c_float, C.c_float, _U64, _P], _I),
     "troute_warm_grad": ([_P, _P, _I, _P, _P], _I),
     "troute_warm_predict": ([_P, _P, _I, _P], _I),
-    "troute_warm_predict_gemm": ([_P, _P, _I, _P], _I),
     "troute_set_warm_start": ([_P, _P, _D], _I),
     "troute_get_pairs": ([_P, _P, C.c_longlong, _P], _I),
     "troute_get_start_history": ([_P, _P, _I], _I),
@@ -866,19 +865,13 @@ class WarmModel:
         return g, loss.value
 
     def predict(self, inputs) -> np.ndarray:
-        """Predicted depths for host rows [n][8] (qup quc qdp ql dx s0 n bw), tensor-core path."""
+        """Predicted depths for host rows [n][8] (qup quc qdp ql dx s0 n bw), through
+        the tcgen05 GEMM that fills a warm-started launch's starting depths."""
         x = np.ascontiguousarray(inputs, np.float32).reshape(-1, 8)
         out = np.zeros(x.shape[0])
         _check(lib().troute_warm_predict(self._h, _ptr(x), x.shape[0], _ptr(out)))
         return out
 
-    def predict_gemm(self, inputs) -> np.ndarray:
-        """The same through the tcgen05 GEMM that fills a warm-started launch's
-        starting depths."""
-        x = np.ascontiguousarray(inputs, np.float32).reshape(-1, 8)
-        out = np.zeros(x.shape[0])
-        _check(lib().troute_warm_predict_gemm(self._h, _ptr(x), x.shape[0], _ptr(out)))
-        return out
 
 
 def route_tree(topo: dict, params, qlat_ts, qdp0, dp0, reach_last0=None, dt: float = 300.0, cfg: Cfg | None = None,
