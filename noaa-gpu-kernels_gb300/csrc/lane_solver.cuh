@@ -28,9 +28,16 @@ enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_DONE = 4 };
 // solve: copied once when the solve starts, read by every pass. (Re-reading
 // them from global memory every pass misses L2 once a network's parameters
 // outgrow it -- c1's are 260 MB -- and costs a DRAM round trip per pass.)
-// Layout [plane][thread of the block]: a warp's reads of one plane are 512
-// contiguous bytes, free of bank conflicts.
-constexpr int kSegSmemStride = 128;  // threads per block of the per-lane kernels
+// Layout [warp][plane][lane]: a warp's reads of one plane are 512 contiguous
+// bytes, free of bank conflicts, whatever the block size.
+constexpr int kSegSmemStride = 32;
+
+// This thread's staging slot in a block's array of kParamPlanes x blockDim
+// double2.
+__device__ __forceinline__ double2* seg_slot_of(double2* seg_sm)
+{
+    return seg_sm + (threadIdx.x >> 5) * (kParamPlanes * kSegSmemStride) + (threadIdx.x & 31);
+}
 
 __device__ __forceinline__ void stage_seg(const NetDev& net, long long s, double2* slot)
 {

@@ -25,16 +25,24 @@
 // the reference's given the same coefficients.
 //
 // Step (device): y[r] = sum_k P_Q[r,k] x[k] + sum_k P_q[r,k] ql[k]. The step
-// is HBM-bound (8 bytes per stored entry; the ~4 MB vectors stay in L2). The
-// sum keeps the reference kernel's arithmetic exactly (kernel_spmv_fused,
+// is HBM-bound (8 bytes per stored entry, each entry a (column, value) pair
+// read by one streaming load; the ~4 MB vectors stay in L2). The sum keeps the
+// reference kernel's arithmetic exactly (kernel_spmv_fused,
 // linear_mc_matrix_graph.cu:174-206: lane l of 32 accumulates entries l,
 // l + 32, ... of each matrix by fused multiply-add, adds the two partials,
-// then the shuffle-down tree 16, 8, 4, 2, 1), but with 8 lanes per row: lane p
-// holds the reference's lanes p, p + 8, p + 16, p + 24, performs the tree's
-// first two levels in registers in the same pairing ((p + (p+16)) +
-// ((p+8) + (p+24))) and the last three by shuffles inside its 8-lane group.
-// Rows hold ~18 entries on average, so a warp covers 4 rows instead of 1
-// with 14 of 32 lanes busy.
+// then the shuffle-down tree 16, 8, 4, 2, 1). Row lengths are heavily skewed
+// (on a 1.1 M-reach network the median row holds 1 entry, 14 % of rows hold
+// more than 32 and those hold 80 % of the entries), so rows take one of two
+// paths:
+//  - short rows (at most 32 entries in each matrix) by 8 lanes: lane p holds
+//    the reference's lanes p, p + 8, p + 16, p + 24, performs the tree's
+//    first two levels in registers in the same pairing ((p + (p+16)) +
+//    ((p+8) + (p+24))) and the last three by shuffles in its 8-lane group;
+//    a warp covers 4 rows;
+//  - long rows by the whole warp, lane l being the reference's lane l, each
+//    lane issuing the loads of several of its entries before it gathers and
+//    adds them, so a row of hundreds of entries costs a few memory round
+//    trips instead of one per entry.
 //
 // A run of n_ts steps is recorded once as a CUDA graph of n_ts launches
 // (alternating two discharge buffers) and replayed while the caller's
@@ -54,8 +62,19 @@ namespace tr {
 namespace {
 
 constexpr unsigned kFullMask = 0xffffffffu;
-constexpr int kMatThreads = 256;
-constexpr int kLanesPerRow = 8;
+#ifndef TROUTE_MAT_THREADS
+#define TROUTE_MAT_THREADS 256
+#endif
+#ifndef TROUTE_MAT_LONG_BATCH
+#define TROUTE_MAT_LONG_BATCH 4
+#endif
+#ifndef TROUTE_MAT_LANES
+#define TROUTE_MAT_LANES 8
+#endif
+constexpr int kMatThreads = TROUTE_MAT_THREADS;
+constexpr int kLanesPerRow = TROUTE_MAT_LANES;   // lanes of a short row
+constexpr int kRefPerLane = 32 / kLanesPerRow;   // the reference's lanes each of them holds
+static_assert(kLanesPerRow >= 2 && kLanesPerRow <= 16 && 32 % kLanesPerRow == 0, "lanes per short row");
 constexpr int kRowsPerBlock = kMatThreads / kLanesPerRow;
 
 // Coefficients of one reach at X = 0.25 (linear_mc_matrix.cu:56-86), FP32 in
@@ -91,72 +110,126 @@ __global__ void mat_coeff_kernel(const troute_chparams_f32* __restrict__ p, int 
 struct MatDev {
     int R;
     const int* qp;     // P_Q row pointers [R + 1]
-    const int* qc;     // P_Q columns
-    const float* qv;   // P_Q values
+    const int2* qe;    // P_Q entries: (column, value bits)
     const int* lp;     // P_q row pointers [R + 1]
-    const int* lc;
-    const float* lv;
+    const int2* le;    // P_q entries
 };
 
-// Continues the reference's lane `v` over one matrix row [b, e) from entry
-// k0 on: entries k0, k0 + 32, ... accumulated by fused multiply-add onto s.
-__device__ __forceinline__ float lane_tail(const int* __restrict__ col, const float* __restrict__ val,
-                                           const float* __restrict__ vec, int k0, int e, float s)
+// A row whose two matrices hold at most this many entries each is summed by
+// an 8-lane group (one entry per reference lane at most); longer rows by the
+// whole warp.
+constexpr int kShortRow = 32;
+// Entries a lane loads per matrix before it gathers and adds, on long rows.
+constexpr int kLongBatch = TROUTE_MAT_LONG_BATCH;
+
+// Entries are read once per step: streaming loads, evicted first, so the
+// gathered discharge and inflow vectors keep their place in L2.
+__device__ __forceinline__ int2 ld_entry(const int2* __restrict__ e, int k) { return __ldcs(e + k); }
+
+// Sum of one long row by the whole warp: lane l is the reference's lane l
+// (entries l, l + 32, ... of each matrix, fused multiply-add from 0, the two
+// partials added, then the shuffle-down tree 16, 8, 4, 2, 1); each lane loads
+// kLongBatch entries of each matrix, then gathers them, then adds them in
+// order. Returns the row's value in lane 0.
+__device__ __forceinline__ float long_row(const MatDev& m, const float* __restrict__ x, const float* __restrict__ ql,
+                                          int lane, int qb, int nq, int lb, int nl)
 {
-    for (int k = k0; k < e; k += 32) s = __fmaf_rn(__ldg(val + k), __ldg(vec + __ldg(col + k)), s);
-    return s;
+    float sq = 0.0f, sl = 0.0f;
+    const int n = max(nq, nl);
+    for (int k = lane; k < n; k += kLongBatch * 32) {
+        int2 eq[kLongBatch], el[kLongBatch];
+#pragma unroll
+        for (int j = 0; j < kLongBatch; ++j) {
+            const int kk = k + 32 * j;
+            eq[j] = kk < nq ? ld_entry(m.qe, qb + kk) : make_int2(0, 0);
+            el[j] = kk < nl ? ld_entry(m.le, lb + kk) : make_int2(0, 0);
+        }
+        float xq[kLongBatch], xl[kLongBatch];
+#pragma unroll
+        for (int j = 0; j < kLongBatch; ++j) {
+            const int kk = k + 32 * j;
+            xq[j] = kk < nq ? __ldg(x + eq[j].x) : 0.0f;
+            xl[j] = kk < nl ? __ldg(ql + el[j].x) : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < kLongBatch; ++j) {
+            const int kk = k + 32 * j;
+            if (kk < nq) sq = __fmaf_rn(__int_as_float(eq[j].y), xq[j], sq);
+            if (kk < nl) sl = __fmaf_rn(__int_as_float(el[j].y), xl[j], sl);
+        }
+    }
+    float u = __fadd_rn(sq, sl);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) u = __fadd_rn(u, __shfl_down_sync(kFullMask, u, off));
+    return u;
 }
 
 __global__ void __launch_bounds__(kMatThreads) mat_step_kernel(MatDev m, const float* __restrict__ x,
                                                                const float* __restrict__ ql, float* __restrict__ y)
 {
-    const int p = threadIdx.x & (kLanesPerRow - 1);
+    const int lane = threadIdx.x & 31;
+    const int p = lane & (kLanesPerRow - 1);
     const int row = blockIdx.x * kRowsPerBlock + threadIdx.x / kLanesPerRow;
-    float u = 0.0f;
+    int qb = 0, nq = 0, lb = 0, nl = 0;
     if (row < m.R) {
-        const int qb = __ldg(m.qp + row), qe = __ldg(m.qp + row + 1);
-        const int lb = __ldg(m.lp + row), le = __ldg(m.lp + row + 1);
-        // the first entry of each of the reference's lanes p, p+8, p+16, p+24
-        // (rows of up to 32 entries have no other): every column and value
-        // load is issued before any gather, and every gather before any sum,
-        // so a row costs two memory round trips instead of a chain of them
-        int cq[4], cl[4];
-        float vq[4], vl[4];
+        qb = __ldg(m.qp + row);
+        nq = __ldg(m.qp + row + 1) - qb;
+        lb = __ldg(m.lp + row);
+        nl = __ldg(m.lp + row + 1) - lb;
+    }
+    const bool is_long = nq > kShortRow || nl > kShortRow;
+    float u = 0.0f;
+    if (!is_long) {
+        // the entry of each of the reference's lanes p, p + kLanesPerRow, ...
+        // (a short row has no other): every entry load is issued before any
+        // gather, and every gather before any sum
+        int2 eq[kRefPerLane], el[kRefPerLane];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int kq = qb + p + kLanesPerRow * j, kl = lb + p + kLanesPerRow * j;
-            cq[j] = kq < qe ? __ldg(m.qc + kq) : 0;
-            vq[j] = kq < qe ? __ldg(m.qv + kq) : 0.0f;
-            cl[j] = kl < le ? __ldg(m.lc + kl) : 0;
-            vl[j] = kl < le ? __ldg(m.lv + kl) : 0.0f;
+        for (int j = 0; j < kRefPerLane; ++j) {
+            const int k = p + kLanesPerRow * j;
+            eq[j] = k < nq ? ld_entry(m.qe, qb + k) : make_int2(0, 0);
+            el[j] = k < nl ? ld_entry(m.le, lb + k) : make_int2(0, 0);
         }
-        float xq[4], xl[4];
+        float xq[kRefPerLane], xl[kRefPerLane];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int kq = qb + p + kLanesPerRow * j, kl = lb + p + kLanesPerRow * j;
-            xq[j] = kq < qe ? __ldg(x + cq[j]) : 0.0f;
-            xl[j] = kl < le ? __ldg(ql + cl[j]) : 0.0f;
+        for (int j = 0; j < kRefPerLane; ++j) {
+            const int k = p + kLanesPerRow * j;
+            xq[j] = k < nq ? __ldg(x + eq[j].x) : 0.0f;
+            xl[j] = k < nl ? __ldg(ql + el[j].x) : 0.0f;
         }
-        float s[4];
+        float s[kRefPerLane];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int kq = qb + p + kLanesPerRow * j, kl = lb + p + kLanesPerRow * j;
+        for (int j = 0; j < kRefPerLane; ++j) {
+            const int k = p + kLanesPerRow * j;
             // fma(v, x, 0) where the lane holds an entry, 0 where it holds none
-            float sq = kq < qe ? __fmaf_rn(vq[j], xq[j], 0.0f) : 0.0f;
-            float sl = kl < le ? __fmaf_rn(vl[j], xl[j], 0.0f) : 0.0f;
-            if (kq + 32 < qe) sq = lane_tail(m.qc, m.qv, x, kq + 32, qe, sq);
-            if (kl + 32 < le) sl = lane_tail(m.lc, m.lv, ql, kl + 32, le, sl);
+            const float sq = k < nq ? __fmaf_rn(__int_as_float(eq[j].y), xq[j], 0.0f) : 0.0f;
+            const float sl = k < nl ? __fmaf_rn(__int_as_float(el[j].y), xl[j], 0.0f) : 0.0f;
             s[j] = __fadd_rn(sq, sl);
         }
-        // shuffle-down levels 16 and 8 of the reference's tree, in registers:
-        // lane v + 16 onto v, then (v + 8) onto v
-        u = __fadd_rn(__fadd_rn(s[0], s[2]), __fadd_rn(s[1], s[3]));
+        // the reference's shuffle-down levels 16 .. kLanesPerRow in registers:
+        // at offset o its lane v adds lane v + o; slot j holds its lane
+        // p + kLanesPerRow j, so offset o adds slot j + o / kLanesPerRow onto j
+#pragma unroll
+        for (int h = kRefPerLane / 2; h >= 1; h >>= 1)
+#pragma unroll
+            for (int j = 0; j < h; ++j) s[j] = __fadd_rn(s[j], s[j + h]);
+        u = s[0];
     }
-    // levels 4, 2, 1 inside the row's 8-lane group (every lane takes part)
-    u = __fadd_rn(u, __shfl_down_sync(kFullMask, u, 4, kLanesPerRow));
-    u = __fadd_rn(u, __shfl_down_sync(kFullMask, u, 2, kLanesPerRow));
-    u = __fadd_rn(u, __shfl_down_sync(kFullMask, u, 1, kLanesPerRow));
-    if (p == 0 && row < m.R) y[row] = u;
+    // the remaining levels inside the row's lane group (every lane takes part)
+#pragma unroll
+    for (int off = kLanesPerRow / 2; off >= 1; off >>= 1)
+        u = __fadd_rn(u, __shfl_down_sync(kFullMask, u, off, kLanesPerRow));
+    if (p == 0 && row < m.R && !is_long) y[row] = u;
+    // the warp's long rows, one after another, each by all 32 lanes
+    unsigned longs = __ballot_sync(kFullMask, is_long && p == 0);
+    while (longs) {
+        const int src = __ffs(longs) - 1;
+        longs &= longs - 1;
+        const int r = __shfl_sync(kFullMask, row, src);
+        const float v = long_row(m, x, ql, lane, __shfl_sync(kFullMask, qb, src), __shfl_sync(kFullMask, nq, src),
+                                 __shfl_sync(kFullMask, lb, src), __shfl_sync(kFullMask, nl, src));
+        if (lane == 0) y[r] = v;
+    }
 }
 
 template <typename T>
@@ -314,14 +387,15 @@ using namespace tr;
 struct troute_matrix {
     int R = 0;
     long long nnz_Q = 0, nnz_q = 0;
-    MArr<int> qp, qc, lp, lc;
-    MArr<float> qv, lv, tmp;
+    MArr<int> qp, lp;
+    MArr<int2> qe, le;
+    MArr<float> tmp;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     const float* g_qlat = nullptr;
     float* g_q = nullptr;
     int g_nts = 0;
-    MatDev dev() const { return MatDev{R, qp.p, qc.p, qv.p, lp.p, lc.p, lv.p}; }
+    MatDev dev() const { return MatDev{R, qp.p, qe.p, lp.p, le.p}; }
     ~troute_matrix()
     {
         if (graph) cudaGraphExecDestroy(graph);
@@ -392,16 +466,29 @@ extern "C" int troute_matrix_create(troute_matrix** out, int n_reaches, const in
     auto up = [&](void* dst, const void* src, size_t bytes) {
         return bytes ? mat_cuda(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "matrix upload") : TROUTE_OK;
     };
-    if ((rc = mat_cuda(cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking), "stream")) ||
-        (rc = M->qp.alloc(R1)) || (rc = M->qc.alloc(PQ.col.size())) || (rc = M->qv.alloc(PQ.val.size())) ||
-        (rc = M->lp.alloc(R1)) || (rc = M->lc.alloc(Pq.col.size())) || (rc = M->lv.alloc(Pq.val.size())) ||
-        (rc = M->tmp.alloc((size_t)std::max(1, n_reaches))) ||
-        (rc = up(M->qp.p, PQ.ptr.data(), R1 * sizeof(int))) ||
-        (rc = up(M->qc.p, PQ.col.data(), PQ.col.size() * sizeof(int))) ||
-        (rc = up(M->qv.p, PQ.val.data(), PQ.val.size() * sizeof(float))) ||
-        (rc = up(M->lp.p, Pq.ptr.data(), R1 * sizeof(int))) ||
-        (rc = up(M->lc.p, Pq.col.data(), Pq.col.size() * sizeof(int))) ||
-        (rc = up(M->lv.p, Pq.val.data(), Pq.val.size() * sizeof(float)))) {
+    // entries as (column, value bits) pairs: one 8-byte load per entry
+    auto pairs = [](const HostCsr& m) {
+        std::vector<int2> e(m.col.size());
+        for (size_t k = 0; k < e.size(); ++k) {
+            int v;
+            std::memcpy(&v, &m.val[k], sizeof v);
+            e[k] = make_int2(m.col[k], v);
+        }
+        return e;
+    };
+    try {
+        const std::vector<int2> eQ = pairs(PQ), eq = pairs(Pq);
+        rc = mat_cuda(cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking), "stream");
+        if (!rc && !(rc = M->qp.alloc(R1)) && !(rc = M->qe.alloc(eQ.size())) && !(rc = M->lp.alloc(R1)) &&
+            !(rc = M->le.alloc(eq.size())) && !(rc = M->tmp.alloc((size_t)std::max(1, n_reaches))) &&
+            !(rc = up(M->qp.p, PQ.ptr.data(), R1 * sizeof(int))) &&
+            !(rc = up(M->qe.p, eQ.data(), eQ.size() * sizeof(int2))) &&
+            !(rc = up(M->lp.p, Pq.ptr.data(), R1 * sizeof(int))))
+            rc = up(M->le.p, eq.data(), eq.size() * sizeof(int2));
+    } catch (const std::bad_alloc&) {
+        rc = set_error(TROUTE_ENOMEM, "matrix upload: host memory");
+    }
+    if (rc) {
         delete M;
         return rc;
     }
@@ -429,15 +516,23 @@ extern "C" int troute_matrix_get(const troute_matrix* M, int which, int* ptr, in
     if (!M || (which != 0 && which != 1)) return set_error(TROUTE_EINVAL, "bad arguments");
     const size_t nnz = (size_t)(which ? M->nnz_q : M->nnz_Q);
     const int* dp = which ? M->lp.p : M->qp.p;
-    const int* dc = which ? M->lc.p : M->qc.p;
-    const float* dv = which ? M->lv.p : M->qv.p;
+    const int2* de = which ? M->le.p : M->qe.p;
     int rc;
     if (ptr && (rc = mat_cuda(cudaMemcpy(ptr, dp, ((size_t)M->R + 1) * sizeof(int), cudaMemcpyDeviceToHost), "D2H")))
         return rc;
-    if (col && nnz && (rc = mat_cuda(cudaMemcpy(col, dc, nnz * sizeof(int), cudaMemcpyDeviceToHost), "D2H")))
-        return rc;
-    if (val && nnz && (rc = mat_cuda(cudaMemcpy(val, dv, nnz * sizeof(float), cudaMemcpyDeviceToHost), "D2H")))
-        return rc;
+    if ((col || val) && nnz) {
+        std::vector<int2> e;
+        try {
+            e.resize(nnz);
+        } catch (const std::bad_alloc&) {
+            return set_error(TROUTE_ENOMEM, "matrix download: host memory");
+        }
+        if ((rc = mat_cuda(cudaMemcpy(e.data(), de, nnz * sizeof(int2), cudaMemcpyDeviceToHost), "D2H"))) return rc;
+        for (size_t k = 0; k < nnz; ++k) {
+            if (col) col[k] = e[k].x;
+            if (val) std::memcpy(&val[k], &e[k].y, sizeof(float));
+        }
+    }
     return TROUTE_OK;
 }
 

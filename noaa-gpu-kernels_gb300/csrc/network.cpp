@@ -274,7 +274,7 @@ static int launch_shape(troute_handle* H)
     if ((rc = cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr"))) return rc;
     H->mapping = H->cfg.mapping ? H->cfg.mapping : 3;
     if (H->mapping == 3) {
-        H->threads = 128;
+        H->threads = route_dataflow_threads();
         if ((rc = route_dataflow_occupancy(&bps, H->cfg.warm_start != 0))) return rc;
     } else if (H->mapping == 2) {
         H->threads = 128;

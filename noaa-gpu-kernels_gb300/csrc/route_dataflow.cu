@@ -102,20 +102,31 @@ __device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base,
     L.mode = begin_segment(L, net, run, ls, hist_s, slot) ? L_SOLVE : L_DONE;
 }
 
-// Resident blocks per SM the register allocation is sized for.
+// Threads per block, and the register budget: resident blocks per SM the
+// allocation is sized for, or (TROUTE_DF_MAXNREG) a register cap.
+#ifndef TROUTE_DF_THREADS
+#define TROUTE_DF_THREADS 128
+#endif
 #ifndef TROUTE_DF_MINB
 #define TROUTE_DF_MINB 1
 #endif
+#ifdef TROUTE_DF_MAXNREG
+#define TROUTE_DF_BOUNDS __maxnreg__(TROUTE_DF_MAXNREG)
+#else
+#define TROUTE_DF_BOUNDS __launch_bounds__(TROUTE_DF_THREADS, TROUTE_DF_MINB)
+#endif
+constexpr int kDfThreads = TROUTE_DF_THREADS;
+static_assert(kDfThreads % 32 == 0 && kDfThreads >= 32 && kDfThreads <= 1024, "whole warps per block");
 
 // Warm-started runs read each solve's learned starting depth from the
 // prediction plane the launch's GEMM filled (warm_gemm.cu) when the solve
 // begins (lane_solver.cuh, begin_segment): the same kernel serves plain and
 // warm-started runs.
-__global__ void __launch_bounds__(128, TROUTE_DF_MINB) route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df)
+__global__ void TROUTE_DF_BOUNDS route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df)
 {
     __shared__ unsigned int hist_s[16];
-    __shared__ double2 seg_sm[kParamPlanes * kSegSmemStride];
-    double2* const seg_slot = seg_sm + threadIdx.x;
+    __shared__ double2 seg_sm[kParamPlanes * kDfThreads];
+    double2* const seg_slot = seg_slot_of(seg_sm);
     if (threadIdx.x < 16) hist_s[threadIdx.x] = 0;
     __syncthreads();
     LocalStats ls = {0, 0, 0, 0, 0, 0};
@@ -375,15 +386,18 @@ int launch_route_dataflow(const NetDev& net, const RunDev& run, const DataflowDe
     if (ig > 4096) ig = 4096;
     if (ig < 1) ig = 1;
     dataflow_init_kernel<<<ig, 256, 0, st>>>(net, run, df);
-    route_dataflow_kernel<<<grid, 128, 0, st>>>(net, run, df);
+    route_dataflow_kernel<<<grid, kDfThreads, 0, st>>>(net, run, df);
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(TROUTE_ECUDA, "route_dataflow_kernel launch: %s", cudaGetErrorString(e));
     return TROUTE_OK;
 }
 
+int route_dataflow_threads() { return kDfThreads; }
+
 int route_dataflow_occupancy(int* blocks_per_sm, bool)
 {
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, route_dataflow_kernel, 128, 0);
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, route_dataflow_kernel, kDfThreads, 0);
     if (e != cudaSuccess) return set_error(TROUTE_ECUDA, "occupancy query: %s", cudaGetErrorString(e));
     return TROUTE_OK;
 }

@@ -50,8 +50,8 @@ __device__ __forceinline__ void publish(Lane& L, const NetDev& net)
 __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
 {
     __shared__ unsigned int hist_s[16];
-    __shared__ double2 seg_sm[kParamPlanes * kSegSmemStride];
-    double2* const slot = seg_sm + threadIdx.x;
+    __shared__ double2 seg_sm[kParamPlanes * 128];
+    double2* const slot = seg_slot_of(seg_sm);
     __shared__ int2 queue[4][kQCap];
     if (threadIdx.x < 16) hist_s[threadIdx.x] = 0;
     __syncthreads();

@@ -181,6 +181,7 @@ bool warm_ready(const troute_warm* w);
 int compact_pairs(const float* dense, long long n_rows, float* out, long long capacity, long long* n_valid,
                   void* stream);
 int route_dataflow_occupancy(int* blocks_per_sm, bool warm);
+int route_dataflow_threads();
 int launch_bump_steps(int* step_base, int n_ts, void* stream);
 int launch_fill_int(int* p, long long n, const int* value_dev, int value_host, void* stream);
 int launch_scatter(const double* src, const long long* map, long long n, double* dst,

@@ -23,7 +23,7 @@
 //   layer 1: D1[128 x 64] = A1[128 x 16] . W1^T   (one tcgen05.mma, K = 16:
 //            the 8 features zero-padded)
 //   layer 2: D2[128 x 64] = A2[128 x 64] . W2^T   (four tcgen05.mma, K = 16
-//            each, accumulating), A2 = bf16(SiLU(D1 + b1))
+//            each, accumulating), A2 = SiLU(D1 + b1) in bf16x2 arithmetic
 //   layer 3: y = b3 + w3 . SiLU(D2 + b2) on the CUDA cores (one output column)
 // BF16 operands from shared memory (no-swizzle K-major canonical layout: 8-row
 // x 16-byte core matrices of 128 contiguous bytes), FP32 accumulation in TMEM
@@ -92,15 +92,20 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
+// A waiting thread is suspended by the hardware until the phase completes (or
+// this long) instead of spinning, leaving the issue slots to the other CTAs'
+// epilogues.
+constexpr uint32_t kSuspendNs = 100000;
+
 __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity)
 {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred P1;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2, %3;\n\t"
         "selp.b32 %0, 1, 0, P1;\n\t}\n"
         : "=r"(done)
-        : "r"(mbar), "r"(parity)
+        : "r"(mbar), "r"(parity), "r"(kSuspendNs)
         : "memory");
     return done != 0;
 }
@@ -118,18 +123,40 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 __device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 16 consecutive FP32 columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+// 64 consecutive FP32 columns of this thread's TMEM lane, one load and one wait.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64])
 {
-    uint32_t r[16];
+    uint32_t r[64];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+        "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+        "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// SiLU of two values as a packed bf16 pair: z rounded to bf16, then t (1 +
+// tanh t) with t = z / 2 in bf16x2 arithmetic (the result feeds a BF16 MMA).
+__device__ __forceinline__ unsigned silu2_bf16(float lo, float hi)
+{
+    const unsigned z = pack_bf16(lo, hi);
+    unsigned t, th, r;
+    asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(t) : "r"(z), "r"(0x3f003f00u));  // z * 0.5
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(th) : "r"(t));
+    asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(r) : "r"(t), "r"(th), "r"(t));  // t + t tanh(t)
+    return r;
 }
 
 // Rows of the GEMM from caller-provided raw inputs [n][8] (one step).
@@ -270,21 +297,18 @@ __global__ void __launch_bounds__(kGRows) warm_gemm_kernel(WarmDev m, Rows rows,
             parity ^= 1u;
             tc_after_sync();
             // ---- SiLU(D1 + b1) -> A2 (bf16) ----
+            {
+                float v[64];
+                tmem_ld64(d1 + lane_off, v);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                float v[16];
-                tmem_ld16(d1 + lane_off + 16 * c, v);
-                uint4 q0, q1;
-                q0.x = pack_bf16(silu(v[0] + S.b1[16 * c + 0]), silu(v[1] + S.b1[16 * c + 1]));
-                q0.y = pack_bf16(silu(v[2] + S.b1[16 * c + 2]), silu(v[3] + S.b1[16 * c + 3]));
-                q0.z = pack_bf16(silu(v[4] + S.b1[16 * c + 4]), silu(v[5] + S.b1[16 * c + 5]));
-                q0.w = pack_bf16(silu(v[6] + S.b1[16 * c + 6]), silu(v[7] + S.b1[16 * c + 7]));
-                q1.x = pack_bf16(silu(v[8] + S.b1[16 * c + 8]), silu(v[9] + S.b1[16 * c + 9]));
-                q1.y = pack_bf16(silu(v[10] + S.b1[16 * c + 10]), silu(v[11] + S.b1[16 * c + 11]));
-                q1.z = pack_bf16(silu(v[12] + S.b1[16 * c + 12]), silu(v[13] + S.b1[16 * c + 13]));
-                q1.w = pack_bf16(silu(v[14] + S.b1[16 * c + 14]), silu(v[15] + S.b1[16 * c + 15]));
-                *reinterpret_cast<uint4*>(&S.a2[tid / 8][2 * c][tid % 8][0]) = q0;
-                *reinterpret_cast<uint4*>(&S.a2[tid / 8][2 * c + 1][tid % 8][0]) = q1;
+                for (int c = 0; c < 8; ++c) {
+                    uint4 q;
+                    q.x = silu2_bf16(v[8 * c + 0] + S.b1[8 * c + 0], v[8 * c + 1] + S.b1[8 * c + 1]);
+                    q.y = silu2_bf16(v[8 * c + 2] + S.b1[8 * c + 2], v[8 * c + 3] + S.b1[8 * c + 3]);
+                    q.z = silu2_bf16(v[8 * c + 4] + S.b1[8 * c + 4], v[8 * c + 5] + S.b1[8 * c + 5]);
+                    q.w = silu2_bf16(v[8 * c + 6] + S.b1[8 * c + 6], v[8 * c + 7] + S.b1[8 * c + 7]);
+                    *reinterpret_cast<uint4*>(&S.a2[tid / 8][c][tid % 8][0]) = q;
+                }
             }
             fence_async_smem();
             tc_before_sync();
@@ -308,12 +332,11 @@ __global__ void __launch_bounds__(kGRows) warm_gemm_kernel(WarmDev m, Rows rows,
             tc_after_sync();
             // ---- layer 3 on the CUDA cores ----
             float y = m.b3;
+            {
+                float v[64];
+                tmem_ld64(d2 + lane_off, v);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                float v[16];
-                tmem_ld16(d2 + lane_off + 16 * c, v);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) y += S.w3[16 * c + j] * silu(v[j] + S.b2[16 * c + j]);
+                for (int j = 0; j < 64; ++j) y += S.w3[j] * silu(v[j] + S.b2[j]);
             }
             if (live) rows.store(row, t, __expf(y * m.sd_y + m.mu_y));
             tc_before_sync();
