@@ -25,25 +25,71 @@ namespace tr {
 enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_DONE = 4 };
 
 // A lane's current segment parameters live in shared memory for the whole
-// solve: copied once when the solve starts, read by every pass. (Re-reading
-// them from global memory every pass misses L2 once a network's parameters
-// outgrow it -- c1's are 260 MB -- and costs a DRAM round trip per pass.)
-// Layout [warp][plane][lane]: a warp's reads of one plane are 512 contiguous
-// bytes, free of bank conflicts, whatever the block size.
+// solve, read by every pass. (Re-reading them from global memory every pass
+// misses L2 once a network's parameters outgrow it -- c1's are 260 MB -- and
+// costs a DRAM round trip per pass.) Each lane has two buffers: while segment
+// i is solved, segment i + 1's parameters, inflow column and scale and (warm
+// start) learned starting depth are copied into the other buffer by cp.async,
+// and its discharge and depth are prefetched into L2 -- all static during the
+// launch or final since the reach's previous step completed -- so the next
+// solve starts after one round trip (the inflow) instead of a chain of them.
+// Buffer of segment i: i & 1. A buffer holds kParamPlanes parameter double2
+// and one {inflow scale, inflow column | learned depth} double2.
+// Layout [warp][buffer][plane][lane]: a warp's reads of one plane are 512
+// contiguous bytes, free of bank conflicts, whatever the block size.
 constexpr int kSegSmemStride = 32;
+constexpr int kSegBufPlanes = kParamPlanes + 1;
+constexpr int kSegBufStride = kSegBufPlanes * kSegSmemStride;   // double2 from buffer 0 to 1
+// double2 of a block's staging array per thread
+constexpr int kSegSmemPerThread = 2 * kSegBufPlanes;
 
-// This thread's staging slot in a block's array of kParamPlanes x blockDim
+// This thread's buffer 0 in a block's array of kSegSmemPerThread x blockDim
 // double2.
 __device__ __forceinline__ double2* seg_slot_of(double2* seg_sm)
 {
-    return seg_sm + (threadIdx.x >> 5) * (kParamPlanes * kSegSmemStride) + (threadIdx.x & 31);
+    return seg_sm + (threadIdx.x >> 5) * (2 * kSegBufStride) + (threadIdx.x & 31);
 }
 
-__device__ __forceinline__ void stage_seg(const NetDev& net, long long s, double2* slot)
+// The buffer of the lane's segment i.
+__device__ __forceinline__ double2* seg_buf(double2* slot, int i) { return slot + (i & 1) * kSegBufStride; }
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Asynchronous global -> shared copies of this thread; a thread waits only for
+// its own (cp.async.wait_all).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Starts the copies of tile slot s's record (and learned depth for step tau)
+// into buffer buf, and the L2 prefetch of its discharge and depth. Only data
+// that no thread writes during the launch goes through the non-coherent
+// cp.async path (the records; the prediction plane, written before the
+// launch); the mutable discharge and depth are read later with ld.cg.
+__device__ __forceinline__ void stage_seg_async(const NetDev& net, const RunDev& run, int tau, long long s,
+                                                double2* buf)
 {
     const SegRec* r = net.seg + s;
 #pragma unroll
-    for (int k = 0; k < kParamPlanes; ++k) slot[k * kSegSmemStride] = __ldg(r->p + k);
+    for (int k = 0; k < kParamPlanes; ++k) cp_async16(buf + k * kSegSmemStride, r->p + k);
+    double2* t = buf + kParamPlanes * kSegSmemStride;
+    cp_async8(&t->x, &r->qscale);
+    int* w = reinterpret_cast<int*>(&t->y);
+    cp_async4(w, &r->qcol);
+    if (run.warm) cp_async4(w + 1, run.start_pred + (size_t)tau * (size_t)net.n_seg_int + s);
+    prefetch_l2(net.q + s);
+    prefetch_l2(net.d + s);
 }
 
 // Lateral inflow of segment s in the step whose inflow row is qlat_row: the
@@ -108,11 +154,18 @@ __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const 
     const double* qlat_row = run.qlat + (size_t)L.tau * (size_t)run.qlat_ld;
     while (L.i < L.ns) {
         L.s = L.base + (long long)L.i * kLanes;
+        double2* const buf = seg_buf(slot, L.i);
+        // segment 0 of an item is staged now; every later segment was staged
+        // while the previous one was solved
+        if (L.i == 0) stage_seg_async(net, run, L.tau, L.s, buf);
+        cp_async_wait_all();
+        if (L.i + 1 < L.ns) stage_seg_async(net, run, L.tau, L.s + kLanes, seg_buf(slot, L.i + 1));
         L.qdp = __ldcg(net.q + L.s);
         const double dpp = __ldcg(net.d + L.s);
-        L.ql = seg_inflow(net, L.s, qlat_row);
-        stage_seg(net, L.s, slot);
-        const SegP p = staged_seg(slot);
+        const double2 tail = buf[kParamPlanes * kSegSmemStride];
+        const long long tw = __double_as_longlong(tail.y);
+        L.ql = __ldg(qlat_row + (int)(unsigned)(tw & 0xffffffffll)) * tail.x;   // column: the low word
+        const SegP p = staged_seg(buf);
         L.qup = (L.i == 0) ? L.qup_head : L.q_up_old;
         L.quc = (L.i == 0) ? L.quc_head : L.q_up_new;
         if (p.n_ch <= 0.0 || p.s0 <= 0.0 || p.z <= 0.0 || p.bw <= 0.0 ||
@@ -141,8 +194,7 @@ __device__ __forceinline__ bool begin_segment(Lane& L, const NetDev& net, const 
             // the learned starting depth of this solve, predicted before the launch:
             // the bracket [p (1 - delta), p (1 + delta)] around a positive normal
             // float p below 1e4 m (0x461c4000), else the plain bracket
-            const float prf = __ldcg(run.start_pred + (size_t)L.tau * (size_t)net.n_seg_int + L.s);
-            const unsigned pb = __float_as_uint(prf);
+            const unsigned pb = (unsigned)((unsigned long long)tw >> 32);   // staged with the record
             if (pb >= 0x00800000u && pb < 0x461c4000u) {
                 const double pr = __longlong_as_double(((long long)((pb >> 23) + 896) << 52) |
                                                        ((long long)(pb & 0x7fffff) << 29));  // exact widening
@@ -166,8 +218,8 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
     const double dt = run.dt;
     const double dt2 = run.dt_half;  // dt / 2 (exact), formed on the host
     if (L.mode == L_SOLVE) {
-        // the segment's parameters, staged in shared memory when the solve began
-        const SegP p = staged_seg(slot);
+        // the segment's parameters, staged in shared memory
+        const SegP p = staged_seg(seg_buf(slot, L.i));
         const double x = L.need0 ? L.h_0 : L.h;  // >= +0
         // Every comparison, minimum and maximum of the pass runs on the integer
         // pipes (fpbits.cuh: the IEEE results, bit for bit), leaving the FP64

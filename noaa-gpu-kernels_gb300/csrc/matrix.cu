@@ -34,15 +34,19 @@
 // (on a 1.1 M-reach network the median row holds 1 entry, 14 % of rows hold
 // more than 32 and those hold 80 % of the entries), so rows take one of two
 // paths:
-//  - short rows (at most 32 entries in each matrix) by 8 lanes: lane p holds
-//    the reference's lanes p, p + 8, p + 16, p + 24, performs the tree's
-//    first two levels in registers in the same pairing ((p + (p+16)) +
-//    ((p+8) + (p+24))) and the last three by shuffles in its 8-lane group;
-//    a warp covers 4 rows;
+//  - short rows (at most 32 entries in each matrix) by 4 lanes: lane p holds
+//    the reference's lanes p, p + 4, ..., p + 28, performs the tree's first
+//    three levels (offsets 16, 8, 4) in registers in the same pairing and the
+//    last two by shuffles in its 4-lane group; a warp covers 8 rows;
 //  - long rows by the whole warp, lane l being the reference's lane l, each
 //    lane issuing the loads of several of its entries before it gathers and
 //    adds them, so a row of hundreds of entries costs a few memory round
 //    trips instead of one per entry.
+// Blocks of 64 threads: a block's slot frees as soon as its two warps finish,
+// so warps held up by long rows do not keep idle warps resident. (Measured
+// on a 1.1 M-reach network, 144 steps: 8 lanes per short row in blocks of
+// 256 22.5 ms, 4 lanes in blocks of 128 16.4 ms, of 64 15.9 ms; 2 lanes
+// 23.6 ms; 8 entries per lane and batch on long rows instead of 4 slower.)
 //
 // A run of n_ts steps is recorded once as a CUDA graph of n_ts launches
 // (alternating two discharge buffers) and replayed while the caller's
@@ -63,13 +67,13 @@ namespace {
 
 constexpr unsigned kFullMask = 0xffffffffu;
 #ifndef TROUTE_MAT_THREADS
-#define TROUTE_MAT_THREADS 256
+#define TROUTE_MAT_THREADS 64
 #endif
 #ifndef TROUTE_MAT_LONG_BATCH
 #define TROUTE_MAT_LONG_BATCH 4
 #endif
 #ifndef TROUTE_MAT_LANES
-#define TROUTE_MAT_LANES 8
+#define TROUTE_MAT_LANES 4
 #endif
 constexpr int kMatThreads = TROUTE_MAT_THREADS;
 constexpr int kLanesPerRow = TROUTE_MAT_LANES;   // lanes of a short row
@@ -116,8 +120,8 @@ struct MatDev {
 };
 
 // A row whose two matrices hold at most this many entries each is summed by
-// an 8-lane group (one entry per reference lane at most); longer rows by the
-// whole warp.
+// a group of kLanesPerRow lanes (one entry per reference lane at most);
+// longer rows by the whole warp.
 constexpr int kShortRow = 32;
 // Entries a lane loads per matrix before it gathers and adds, on long rows.
 constexpr int kLongBatch = TROUTE_MAT_LONG_BATCH;

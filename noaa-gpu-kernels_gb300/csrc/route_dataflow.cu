@@ -125,7 +125,7 @@ static_assert(kDfThreads % 32 == 0 && kDfThreads >= 32 && kDfThreads <= 1024, "w
 __global__ void TROUTE_DF_BOUNDS route_dataflow_kernel(NetDev net, RunDev run, DataflowDev df)
 {
     __shared__ unsigned int hist_s[16];
-    __shared__ double2 seg_sm[kParamPlanes * kDfThreads];
+    __shared__ double2 seg_sm[kSegSmemPerThread * kDfThreads];
     double2* const seg_slot = seg_slot_of(seg_sm);
     if (threadIdx.x < 16) hist_s[threadIdx.x] = 0;
     __syncthreads();
@@ -349,6 +349,7 @@ __global__ void TROUTE_DF_BOUNDS route_dataflow_kernel(NetDev net, RunDev run, D
         atomicAdd(&run.stats->lane_idle, n_idle);
         atomicAdd(&run.stats->solve_passes, n_solve);
     }
+    cp_async_wait_all();   // a lane that left an item early may still have its next segment in flight
     flush_stats(ls, hist_s, run.stats);
 }
 

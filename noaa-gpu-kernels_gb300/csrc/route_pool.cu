@@ -50,7 +50,7 @@ __device__ __forceinline__ void publish(Lane& L, const NetDev& net)
 __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
 {
     __shared__ unsigned int hist_s[16];
-    __shared__ double2 seg_sm[kParamPlanes * 128];
+    __shared__ double2 seg_sm[kSegSmemPerThread * 128];
     double2* const slot = seg_slot_of(seg_sm);
     __shared__ int2 queue[4][kQCap];
     if (threadIdx.x < 16) hist_s[threadIdx.x] = 0;
@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
         atomicAdd(&run.stats->lane_idle, n_idle);
         atomicAdd(&run.stats->solve_passes, n_solve);
     }
+    cp_async_wait_all();   // a lane that left an item early may still have its next segment in flight
     flush_stats(ls, hist_s, run.stats);
 }
 
