@@ -147,8 +147,8 @@ int troute_mc_reach_parallel_device(const troute_chparams* p, const double* ql,
  * solve counters, is an array compiled into the library (about 1.7 MB per
  * GPU, held until the process exits). No counterpart in the reference. At most
  * 2,097,152 reaches per call (larger calls return TROUTE_EINVAL). The first
- * call on a device looks up the array's address with that device current;
- * that first call should come before any stream capture. Calls that overlap
+ * call on a device looks up the array's address with that device current.
+ * Calls that overlap
  * on the GPU share the array and race. With stats non-NULL the call waits for
  * `stream` and returns the counters; only then is a reach with a segment range
  * outside [0, n_segments) reported (TROUTE_EINVAL; its outputs are left

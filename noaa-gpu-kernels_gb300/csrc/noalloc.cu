@@ -15,8 +15,7 @@
 //  - at most kNoAllocMaxBlocks blocks of kNoAllocThreads reaches, i.e.
 //    2,097,152 reaches per call; larger calls are rejected with TROUTE_EINVAL;
 //  - the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; that first call should
-//    come before any stream capture;
+//    (cudaGetSymbolAddress) with that device current;
 //  - all calls share the array and it keeps the last call's contents: calls
 //    whose kernels overlap on the GPU (other streams, other host threads)
 //    race on it. Every counter a call reads is written by that call first, so
