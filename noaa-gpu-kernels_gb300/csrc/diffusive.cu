@@ -36,31 +36,42 @@ struct DiffTiles {
     float qp[kDWarps][kDW][kTileLd];
 };
 
-// Loads nodes [n0, n0 + cnt) (cnt <= 64) of rows r0..r0+31 of `src` into
-// tile[row][k0 + j] (coalesced along the row; nodes outside [0, max_nodes) or
-// rows past n_reaches are left untouched). Eight rows at a time: their loads
-// are all issued before any is stored, so a tile costs four memory round
-// trips, not one per row.
-__device__ __forceinline__ void load_tile(float (*tile)[kTileLd], const float* __restrict__ src, int r0, int n_reaches,
-                                          int max_nodes, int n0, int cnt, int k0, int lane)
+// Loads nodes [n0, n0 + cnt) (cnt <= 64) of rows r0..r0+31 of dx and the
+// diffusivity and nodes [n0, n0 + cnt + 1) of the previous discharge into
+// their tiles, tile[row][j] = node n0 + j (coalesced along the row; nodes
+// outside [0, max_nodes) or rows past n_reaches are left untouched). Eight
+// rows of all three arrays at a time: their loads are all issued before any is
+// stored, so a tile costs four memory round trips for the three arrays.
+__device__ __forceinline__ void load_tiles(DiffTiles& T, int w, const float* __restrict__ dx,
+                                           const float* __restrict__ diffusivity, const float* __restrict__ qp_prev,
+                                           int r0, int n_reaches, int max_nodes, int n0, int cnt, int lane)
 {
     const int na = n0 + lane, nb = n0 + lane + kDW;
-    const bool ok_a = lane < cnt && na >= 0 && na < max_nodes;
-    const bool ok_b = lane + kDW < cnt && nb >= 0 && nb < max_nodes;
+    const bool in_a = na >= 0 && na < max_nodes, in_b = nb >= 0 && nb < max_nodes;
+    const bool ok_a = lane < cnt && in_a, ok_b = lane + kDW < cnt && in_b;          // dx, diffusivity
+    const bool okq_a = lane < cnt + 1 && in_a, okq_b = lane + kDW < cnt + 1 && in_b;  // discharge
     for (int row0 = 0; row0 < kDW; row0 += 8) {
-        float va[8], vb[8];
+        float xa[8], xb[8], da[8], db[8], qa[8], qb[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int r = r0 + row0 + q;
             const bool in = r < n_reaches;
-            va[q] = (in && ok_a) ? __ldg(src + (size_t)r * (size_t)max_nodes + na) : 0.0f;
-            vb[q] = (in && ok_b) ? __ldg(src + (size_t)r * (size_t)max_nodes + nb) : 0.0f;
+            const size_t o = (size_t)r * (size_t)max_nodes;
+            xa[q] = (in && ok_a) ? __ldg(dx + o + na) : 0.0f;
+            xb[q] = (in && ok_b) ? __ldg(dx + o + nb) : 0.0f;
+            da[q] = (in && ok_a) ? __ldg(diffusivity + o + na) : 0.0f;
+            db[q] = (in && ok_b) ? __ldg(diffusivity + o + nb) : 0.0f;
+            qa[q] = (in && okq_a) ? __ldg(qp_prev + o + na) : 0.0f;
+            qb[q] = (in && okq_b) ? __ldg(qp_prev + o + nb) : 0.0f;
         }
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             if (r0 + row0 + q < n_reaches) {
-                if (ok_a) tile[row0 + q][k0 + lane] = va[q];
-                if (ok_b) tile[row0 + q][k0 + lane + kDW] = vb[q];
+                const int t = row0 + q;
+                if (ok_a) T.dx[w][t][lane] = xa[q], T.diff[w][t][lane] = da[q];
+                if (ok_b) T.dx[w][t][lane + kDW] = xb[q], T.diff[w][t][lane + kDW] = db[q];
+                if (okq_a) T.qp[w][t][lane] = qa[q];
+                if (okq_b) T.qp[w][t][lane + kDW] = qb[q];
             }
         }
     }
@@ -101,9 +112,7 @@ __global__ void __launch_bounds__(kDW * kDWarps) diffusive_kernel(const troute_d
     for (int i0 = 0; i0 < nc_max; i0 += kDW) {
         __syncwarp();
         // tile column k holds node i0 - 1 + k
-        load_tile(T.dx[w], dx, r0, n_reaches, max_nodes, i0 - 1, kDW + 1, 0, lane);
-        load_tile(T.diff[w], diffusivity, r0, n_reaches, max_nodes, i0 - 1, kDW + 1, 0, lane);
-        load_tile(T.qp[w], qp_prev, r0, n_reaches, max_nodes, i0 - 1, kDW + 2, 0, lane);
+        load_tiles(T, w, dx, diffusivity, qp_prev, r0, n_reaches, max_nodes, i0 - 1, kDW + 1, lane);
         __syncwarp();
         if (live) {
             for (int k = 1; k <= kDW; ++k) {

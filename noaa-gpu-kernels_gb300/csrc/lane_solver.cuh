@@ -22,7 +22,9 @@
 
 namespace tr {
 
-enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_DONE = 4 };
+// L_BEGIN: the lane's next segment (L.i) starts at the kernel's one
+// begin_segment call site before the next evaluation pass.
+enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_BEGIN = 3, L_DONE = 4 };
 
 // A lane's current segment parameters live in shared memory for the whole
 // solve, read by every pass. (Re-reading them from global memory every pass
@@ -390,7 +392,7 @@ __device__ __forceinline__ void lane_pass(Lane& L, const NetDev& net, const RunD
                         o.early = 0;
                         count_solve(ls, hist_s, o);
                         ++L.i;
-                        L.mode = begin_segment(L, net, run, ls, hist_s, slot) ? L_SOLVE : L_DONE;
+                        L.mode = L.i < L.ns ? L_BEGIN : L_DONE;
                     }
                 }
             }

@@ -99,7 +99,7 @@ __device__ __forceinline__ void start_item(Lane& L, int ri, int tau, int t_base,
     L.q_up_new = 0.0;
     L.q_last = 0.0;
     L.i = 0;
-    L.mode = begin_segment(L, net, run, ls, hist_s, slot) ? L_SOLVE : L_DONE;
+    L.mode = L_BEGIN;
 }
 
 // Threads per block, and the register budget: resident blocks per SM the
@@ -252,6 +252,9 @@ __global__ void TROUTE_DF_BOUNDS route_dataflow_kernel(NetDev net, RunDev run, D
                 }
             }
         }
+
+        // ---- lanes starting a segment (the one inlined begin_segment) ----
+        if (L.mode == L_BEGIN) L.mode = begin_segment(L, net, run, ls, hist_s, seg_slot) ? L_SOLVE : L_DONE;
 
         // ---- one depth evaluation per solving lane ----
         if (__any_sync(kFullMask, L.mode >= L_SOLVE)) {

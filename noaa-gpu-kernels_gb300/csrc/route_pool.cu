@@ -147,15 +147,20 @@ __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
                 L.q_up_new = 0.0;
                 L.q_last = 0.0;
                 L.i = 0;
-                if (begin_segment(L, net, run, ls, hist_s, slot)) {
-                    L.mode = L_SOLVE;
-                } else {
-                    publish(L, net);
-                    L.mode = L_IDLE;
-                }
+                L.mode = L_BEGIN;
             } else if (clock64() - L.wait_t0 > run.wait_cycles) {
                 record_error(run.stats, TROUTE_ETIMEOUT, L.ri, L.g, 1);
                 failed = true;
+            }
+        }
+
+        // ---- lanes starting a segment (the one inlined begin_segment) ----
+        if (L.mode == L_BEGIN) {
+            if (begin_segment(L, net, run, ls, hist_s, slot)) {
+                L.mode = L_SOLVE;
+            } else {
+                publish(L, net);
+                L.mode = L_IDLE;
             }
         }
 
