@@ -396,8 +396,8 @@ int troute_matrix_route(int n_reaches, const int* reach_up_ptr, const int* reach
  * linear_mc.cu): fixed per-segment coefficients C1, C2, C3, C4/ql from the
  * channel at half bankfull depth (linear_mc.cu:57-100), then per step
  * Q_new = C1 Q_up_new + C2 Q_up_old + C3 Q_old + (C4/ql) qlat in topological
- * order (cpu_linear_mc, :177-232), FP32. No secant iteration; the secant
- * path is its judge. Every reach needs at least one segment. */
+ * order (cpu_linear_mc, :177-232), FP32. No secant iteration; its error is
+ * measured against the secant path. Every reach needs at least one segment. */
 typedef struct troute_linear troute_linear;
 /* Coefficients for n segments, computed on the device (FP32, CUDA powf/sqrtf
  * as the reference's kernel_precompute_coeffs). Host arrays. */

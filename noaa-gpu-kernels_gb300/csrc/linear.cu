@@ -1,6 +1,6 @@
 // Linearised Muskingum-Cunge: the reference's fast approximate mode
 // (water-prediction/t-route/wavefront/linear_mc.cu), with the secant path as
-// its judge.
+// the yardstick of its error.
 //
 // Per segment, once: C1..C3 and C4/ql from the channel at a reference depth
 // of half bankfull (at least 0.1 m) with X from the Cunge formula at zero

@@ -7,7 +7,7 @@ for bit), and against the golden fixture those produced. GPU: the dataflow
 kernel against the fixture and the oracle (bit for bit, given the same
 coefficients), the device coefficients against the oracle's (CUDA's powf and
 the C library's differ in the last bits), chunked runs, and the secant path
-as the judge of the linear form's error.
+as the yardstick of the linear form's error.
 """
 import os
 
@@ -98,8 +98,8 @@ def test_chunked_device_runs_equal_one_run():
 
 
 @pytest.mark.gpu
-def test_linear_form_judged_by_the_secant_path():
-    """The secant routing is the judge: the linear form's discharge after a
+def test_linear_form_measured_against_the_secant_path():
+    """The secant routing is the yardstick: the linear form's discharge after a
     day of steps, relative to the secant path's on the same inputs, is
     reported and sanity-checked (finite, same total order of magnitude)."""
     c, p32, ql, q0 = synthetic(seed=9, segs=5000, n_ts=48)

@@ -12,7 +12,7 @@ cpu_linear_mc on one-segment-per-reach networks given the same coefficients
 GPU: the library's matrices (host build) and routed discharge (fused step
 kernel, odd and even step counts, graph replays) bit for bit against the
 fixture and the oracle; device coefficients within float rounding of the C
-library's; the matrix form judged by the secant path.
+library's; the matrix form measured against the secant path.
 """
 import os
 
@@ -82,6 +82,59 @@ def test_oracle_rejects_reaches_not_numbered_upstream_first():
     c = [np.ones(2, np.float32) * 0.3] * 4
     with pytest.raises(ValueError):
         O.matrix_build(up_ptr, up_idx, c)
+
+
+def _f32_products(v, x):
+    """fma(v, x, +0) in float32: the product of two floats is exact in
+    double, rounded once; adding +0 turns a -0 product into +0 as the fused
+    operation does."""
+    return (np.float32(v) * np.float32(x)).astype(np.float32) + np.float32(0.0)
+
+
+def _reference_short_row(pq, pl):
+    """The reference kernel's sum of one row with at most 32 entries per
+    matrix: lane l holds its entry l of each matrix (0 where it has none),
+    adds the two, then the shuffle-down tree 16, 8, 4, 2, 1."""
+    s = (np.pad(pq, (0, 32 - len(pq))) + np.pad(pl, (0, 32 - len(pl)))).astype(np.float32)
+    for off in (16, 8, 4, 2, 1):
+        s[:off] = s[:off] + s[off:2 * off]
+    return s[0]
+
+
+def _lane_group_short_row(pq, pl, G):
+    """The library's form with G lanes per row: lane p holds the reference's
+    lanes p, p + G, ...; the tree levels 16 .. G in its registers (offset o
+    adds slot j + o / G onto j), then shuffles G/2 .. 1 across the group."""
+    s = (np.pad(pq, (0, 32 - len(pq))) + np.pad(pl, (0, 32 - len(pl)))).astype(np.float32)
+    J = 32 // G
+    u = np.empty(G, np.float32)
+    for p in range(G):
+        slot = s[p::G].copy()          # slot j = reference lane p + G j
+        h = J // 2
+        while h >= 1:
+            slot[:h] = slot[:h] + slot[h:2 * h]
+            h //= 2
+        u[p] = slot[0]
+    off = G // 2
+    while off >= 1:
+        u[:off] = u[:off] + u[off:2 * off]
+        off //= 2
+    return u[0]
+
+
+def test_lane_groups_sum_short_rows_in_the_reference_order():
+    """The step kernel's short-row mapping (4 lanes per row, the tree's first
+    levels in registers) equals the reference kernel's 32-lane tree bit for
+    bit, for every group width the kernel can be built with."""
+    rng = np.random.default_rng(12)
+    for _ in range(3000):
+        nq, nl = rng.integers(0, 33, 2)
+        scale = 10.0 ** rng.uniform(-6, 6)
+        pq = _f32_products(rng.standard_normal(nq) * scale, rng.standard_normal(nq))
+        pl = _f32_products(rng.standard_normal(nl), rng.standard_normal(nl) * scale)
+        want = _reference_short_row(pq, pl)
+        for G in (2, 4, 8, 16):
+            assert _lane_group_short_row(pq, pl, G).tobytes() == want.tobytes(), (nq, nl, G)
 
 
 def one_segment_topo(up_ptr, R):
@@ -170,8 +223,8 @@ def test_rejects_reaches_not_numbered_upstream_first():
 
 
 @pytest.mark.gpu
-def test_matrix_form_judged_by_the_secant_path():
-    """The secant routing judges the approximate form: on a one-segment-per-
+def test_matrix_form_measured_against_the_secant_path():
+    """The secant routing is the yardstick of the approximate form: on a one-segment-per-
     reach network the matrix form's discharge after a day of steps is set
     against the FP64 secant path's on the same inputs (reported, and sanity-
     checked: finite, same total order of magnitude)."""
