@@ -149,6 +149,45 @@ CRPOW_HD bool crpow_near_midpoint(double s, double err)
     return eb > thr;
 }
 
+// The accurate path of pow23_53 for arguments the rounding test sends there:
+// one more Newton step for r = y^(-1/3), the residual correction again, and
+// the exponent-offset terms from a double-precision log of x = y 2^(3k).
+// Returns {x^(2/3), x^(5/3)} before the scaling by 2^(2k), 2^(5k). On the
+// device it is a separate function: it runs for a tiny share of the
+// arguments, and out of line it keeps the solver's loop body small.
+#if defined(__CUDA_ARCH__)
+static __device__ __noinline__
+#else
+static inline
+#endif
+double2 crpow_accurate(double y, double r, double s, double se, int k)
+{
+    const double third = 1.0 / 3.0;
+    const double r3 = (r * r) * r;
+    const double g = fma(-y, r3, 1.0);
+    const double rr = fma(r * g, third, r);
+    const double zz = y * rr;
+    const double pp = zz * zz;
+    const double ppe = fma(zz, zz, -pp);
+    const double qq = zz * pp;
+    const double qqe = fma(zz, pp, -qq);
+    const double tt = zz * ppe;
+    const double dd = (qq - s) + ((qqe + tt) - se);
+    const double rr2 = rr * rr;
+    const double dl = -(dd * (rr2 * rr2)) * third;
+#if defined(__CUDA_ARCH__)
+    const double lnx = log(y) + (double)(3 * k) * 0.6931471805599453;
+#else
+    const double lnx = std::log(y) + (double)(3 * k) * 0.6931471805599453;
+#endif
+    double2 out;
+    out.x = zz + (dl + zz * (kFl23Minus23 * lnx));
+    const double ww = y * zz;
+    const double wwe = fma(y, zz, -ww);
+    out.y = ww + ((wwe + y * dl) + ww * (kFl53Minus53 * lnx));
+    return out;
+}
+
 // x^fl(2/3) and x^fl(5/3), both correctly rounded (see above). x < 0 gives NaN,
 // x = 0 gives 0, +inf gives +inf, NaN propagates, like pow().
 CRPOW_HD void pow23_53(double x, double* p23, double* p53)
@@ -232,29 +271,9 @@ CRPOW_HD void pow23_53(double x, double* p23, double* p53)
     double z53 = w0 + a53;
     // rounding test (Fast2Sum: z >= |a23|, w0 >= |a53|, so the errors are exact)
     if (crpow_near_midpoint(z23, a23 - (z23 - z)) || crpow_near_midpoint(z53, a53 - (z53 - w0))) {
-        // one more Newton step for r, the residual correction again, and the
-        // offset terms from a double-precision log of x
-        const double r3 = (r * r) * r;
-        const double g = fma(-y, r3, 1.0);
-        const double rr = fma(r * g, third, r);
-        const double zz = y * rr;
-        const double pp = zz * zz;
-        const double ppe = fma(zz, zz, -pp);
-        const double qq = zz * pp;
-        const double qqe = fma(zz, pp, -qq);
-        const double tt = zz * ppe;
-        const double dd = (qq - s) + ((qqe + tt) - se);
-        const double rr2 = rr * rr;
-        const double dl = -(dd * (rr2 * rr2)) * third;
-#if defined(__CUDA_ARCH__)
-        const double lnx = log(y) + (double)(3 * k) * 0.6931471805599453;
-#else
-        const double lnx = std::log(y) + (double)(3 * k) * 0.6931471805599453;
-#endif
-        z23 = zz + (dl + zz * (kFl23Minus23 * lnx));
-        const double ww = y * zz;
-        const double wwe = fma(y, zz, -ww);
-        z53 = ww + ((wwe + y * dl) + ww * (kFl53Minus53 * lnx));
+        const double2 acc = crpow_accurate(y, r, s, se, k);
+        z23 = acc.x;
+        z53 = acc.y;
     }
     *p23 = crpow_scale(z23, 2 * k);
     *p53 = crpow_scale(z53, 5 * k);

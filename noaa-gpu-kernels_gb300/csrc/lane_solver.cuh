@@ -23,8 +23,10 @@
 namespace tr {
 
 // L_BEGIN: the lane's next segment (L.i) starts at the kernel's one
-// begin_segment call site before the next evaluation pass.
-enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_BEGIN = 3, L_DONE = 4 };
+// begin_segment call site before the next evaluation pass; L_START: the lane
+// holds an item (L.ri, L.tau) whose inputs are final, started at the kernel's
+// one start_item call site. Modes from L_SOLVE up count as busy.
+enum : int { L_IDLE = 0, L_WAIT = 1, L_SOLVE = 2, L_BEGIN = 3, L_DONE = 4, L_START = 5 };
 
 // A lane's current segment parameters live in shared memory for the whole
 // solve, read by every pass. (Re-reading them from global memory every pass

@@ -237,7 +237,9 @@ __global__ void TROUTE_DF_BOUNDS route_dataflow_kernel(NetDev net, RunDev run, D
                 failed = true;
             } else if (ri >= 0) {
                 __threadfence();  // the item's inputs were published before it was queued
-                start_item(L, ri, tau, t_base, net, run, df, ls, hist_s, seg_slot);
+                L.ri = ri;
+                L.tau = tau;
+                L.mode = L_START;
             } else if (clock64() - L.wait_t0 > run.wait_cycles) {
                 // a slot can legitimately stay empty for long while the run
                 // advances; give up only if no item completed during a whole
@@ -253,7 +255,9 @@ __global__ void TROUTE_DF_BOUNDS route_dataflow_kernel(NetDev net, RunDev run, D
             }
         }
 
-        // ---- lanes starting a segment (the one inlined begin_segment) ----
+        // ---- lanes starting an item, then a segment (the one inlined
+        // start_item and begin_segment) ----
+        if (L.mode == L_START) start_item(L, L.ri, L.tau, t_base, net, run, df, ls, hist_s, seg_slot);
         if (L.mode == L_BEGIN) L.mode = begin_segment(L, net, run, ls, hist_s, seg_slot) ? L_SOLVE : L_DONE;
 
         // ---- one depth evaluation per solving lane ----
@@ -295,9 +299,10 @@ __global__ void TROUTE_DF_BOUNDS route_dataflow_kernel(NetDev net, RunDev run, D
                 const int2 mine = (npush == 2) ? push1 : push0;
                 if (npush == 2) push1 = make_int2(-1, -1);
                 --npush;
-                start_item(L, mine.x, mine.y, t_base, net, run, df, ls, hist_s, seg_slot);
-                // a reach without solve work completes at once; it is published
-                // in the next pass
+                // started in the next pass, before its evaluation
+                L.ri = mine.x;
+                L.tau = mine.y;
+                L.mode = L_START;
             }
         }
         // warp-aggregated append to the ready queue
