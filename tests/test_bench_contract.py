@@ -104,3 +104,26 @@ def test_shares_of_the_batched_workloads():
     parts = [b.shard("c2", type("D", (), {"world": 3, "rank": r})) for r in range(3)]
     assert share == parts[1] and sorted(i for p in parts for i in p) == list(range(256))
     assert b.shard("c1", D) is None
+
+
+def test_profiles_carry_the_figures_the_bench_reads():
+    """The roofline figures bench.py takes from the committed ncu summaries:
+    each file exists, holds its `key: value` line once, and the value is in a
+    plausible range (FP64 warp instructions per solving pass, DRAM bytes per
+    segment-step of the single-network and ensemble captures, DRAM bytes of
+    one matrix step)."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    want = {
+        ("fp64_instr_per_solving_pass", "route_dataflow_instmix_tree200k.md"): (150.0, 400.0),
+        ("dram_bytes_per_seg_step", "route_kernel_c1.md"): (112.0, 2000.0),
+        ("dram_bytes_per_seg_step", "route_dataflow_warm_ens256.md"): (112.0, 2000.0),
+        ("fp64_pipe_active_pct", "route_dataflow_warm_ens256.md"): (1.0, 100.0),
+        ("dram_bytes_per_step", "mat_step_c1.md"): (3.0e8, 4.0e8),
+    }
+    for (key, name), (lo, hi) in want.items():
+        text = open(os.path.join(ROOT, "profiles", name)).read()
+        assert sum(ln.strip().startswith(key + ":") for ln in text.splitlines()) == 1, (key, name)
+        value, src = bench.profiled_file(key, name)
+        assert src == name and value is not None and lo <= value <= hi, (key, name, value)
