@@ -61,8 +61,6 @@ __global__ void __launch_bounds__(128) route_pool_kernel(NetDev net, RunDev run)
     const unsigned lt = lanemask_lt();
     const int t_base = __ldg(run.step_base);
     const int T = run.n_ts;
-    const Tol tol = run.tol;
-    const double dt = run.dt;
     unsigned q_head = 0, q_tail = 0;  // warp-uniform
     bool exhausted = false;
     bool failed = false;
