@@ -76,6 +76,49 @@ def test_oracle_matches_compiled_reference(segs, seed, tol):
     assert_same_matrices(O.matrix_build(up_ptr, up_idx, co, tol), O.matrix_build(up_ptr, up_idx, co, tol, use_ref=True))
 
 
+def _shape(kind, R):
+    """Upstream CSR of special networks: a chain (reach r drains r - 1), a star
+    (every other reach drains into the last one), a binary comb."""
+    if kind == "chain":
+        return np.array([0] + list(range(R)), np.int32), np.arange(R - 1, dtype=np.int32)
+    if kind == "star":
+        return np.array([0] * R + [R - 1], np.int32), np.arange(R - 1, dtype=np.int32)
+    if kind == "comb":   # reach r (odd) drains a headwater r - 1 and the previous spine reach r - 2
+        ups, ptr = [], [0]
+        for r in range(R):
+            if r % 2 == 1:
+                ups += [r - 1] + ([r - 2] if r >= 3 else [])
+            ptr.append(len(ups))
+        return np.array(ptr, np.int32), np.array(ups, np.int32)
+    raise ValueError(kind)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="needs the reference checkout (compiled reference)")
+@pytest.mark.parametrize("kind,R,tol", [("chain", 3000, 1e-7), ("chain", 200, 0.0), ("star", 2000, 1e-7),
+                                        ("comb", 4001, 1e-7), ("chain", 1, 1e-7)])
+def test_oracle_matches_compiled_reference_on_special_shapes(kind, R, tol):
+    """Long rows (a chain accumulates its whole truncated ancestry; with tol 0
+    nothing is dropped), one very wide row (a star), a single reach: the
+    oracle's build and routing against the reference's build_propagation_matrices."""
+    up_ptr, up_idx = _shape(kind, R)
+    _, _, p32, _, _ = reach_level(max(4 * R, 2000), 21)   # a tree of more than R reaches: their records
+    assert len(p32) >= R
+    p32 = np.ascontiguousarray(p32[:R])
+    c = O.matrix_coeffs(p32)
+    m = O.matrix_build(up_ptr, up_idx, c, tol)
+    assert_same_matrices(m, O.matrix_build(up_ptr, up_idx, c, tol, use_ref=True))
+    lens = np.diff(m[0][0])
+    if kind == "star":
+        assert lens[-1] == R     # C2 at every upstream reach and C3 at itself: the step's whole-warp path
+    if kind == "chain" and tol == 0.0:
+        assert (lens == np.arange(1, R + 1)).all()   # nothing dropped: row r holds reaches 0..r
+    rng = np.random.default_rng(R)
+    ql = rng.uniform(0.0, 2.0, (6, R)).astype(np.float32)
+    q0 = rng.uniform(0.05, 20.0, R).astype(np.float32)
+    q = O.matrix_route(m[0], m[1], ql, q0)
+    assert np.isfinite(q).all()
+
+
 def test_oracle_rejects_reaches_not_numbered_upstream_first():
     up_ptr = np.array([0, 1, 1], np.int32)
     up_idx = np.array([1], np.int32)     # reach 0's upstream reach is reach 1
