@@ -82,6 +82,53 @@ def test_wavefront_matches_compiled_reference_other_seed():
     np.testing.assert_array_equal(o["reach_last"], rlr)
 
 
+def _special_topo(kind, R, rng):
+    """Reach topologies the random trees rarely produce: a chain (reach r
+    drains r - 1), a star (every other reach drains into the last), a single
+    reach; 1-6 segments per reach."""
+    if kind == "chain":
+        up_ptr, up_idx = [0] + list(range(R)), list(range(R - 1))
+    elif kind == "star":
+        up_ptr, up_idx = [0] * R + [R - 1], list(range(R - 1))
+    else:
+        R, up_ptr, up_idx = 1, [0, 0], []
+    seg_len = rng.integers(1, 7, R).astype(np.int32)
+    seg_start = np.concatenate([[0], np.cumsum(seg_len)[:-1]]).astype(np.int32)
+    return {"n_segments": int(seg_len.sum()), "reach_seg_start": seg_start, "reach_seg_len": seg_len,
+            "reach_up_ptr": np.array(up_ptr, np.int32), "reach_up_idx": np.array(up_idx or [0], np.int32)[:len(up_idx)]}
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference checkout not present")
+@pytest.mark.parametrize("kind,R", [("chain", 400), ("star", 300), ("single", 1)])
+def test_wavefront_matches_compiled_reference_on_special_shapes(kind, R):
+    """A 400-reach chain (a critical path as long as the network), a star
+    whose outlet sums 299 upstream outflows, a single reach; with dry
+    segments (zero inflow and state) and segments of invalid parameters
+    (the reference's early exits) mixed in."""
+    from troute_gb300 import synth
+
+    rng = np.random.default_rng(R)
+    t = _special_topo(kind, R, rng)
+    S = t["n_segments"]
+    base = synth.network("tree:3000", seed=98, n_ts=2)
+    p32 = np.asarray(base["params"].view("<f8").reshape(-1, 8), np.float32)
+    p32 = np.ascontiguousarray(p32[rng.integers(0, len(p32), S)])
+    p32[rng.random(S) < 0.03, 4] = 0.0           # n_ch = 0: invalid parameters, an early exit
+    T = 10
+    ql32 = rng.uniform(0.0, 3.0, (T, S)).astype(np.float32)
+    q0 = rng.uniform(0.0, 15.0, S).astype(np.float32)
+    d0 = rng.uniform(0.3, 3.0, S).astype(np.float32)
+    dry = rng.random(S) < 0.05                     # no flow at all: the other early exit
+    ql32[:, dry] = 0.0
+    q0[dry] = 0.0
+    r0 = rng.uniform(0.0, 10.0, len(t["reach_seg_len"])).astype(np.float32)
+    qr, rlr = O.ref_wavefront_fp64(t, p32, ql32, q0, d0, r0)
+    o = O.route_tree(t, p32.astype(np.float64), ql32.astype(np.float64), q0.astype(np.float64),
+                     d0.astype(np.float64), r0.astype(np.float64))
+    np.testing.assert_array_equal(o["q"], qr)
+    np.testing.assert_array_equal(o["reach_last"], rlr)
+
+
 def test_threaded_oracle_identical():
     from troute_gb300 import synth
 
