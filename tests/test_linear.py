@@ -58,6 +58,34 @@ def test_oracle_matches_compiled_reference():
     np.testing.assert_array_equal(qo, qr)
 
 
+@pytest.mark.skipif(not O.ref_available(), reason="needs the reference checkout (compiled reference)")
+@pytest.mark.parametrize("kind,R", [("chain", 500), ("star", 300), ("single", 1)])
+def test_oracle_matches_compiled_reference_on_special_shapes(kind, R):
+    """A 500-reach chain (one reach per level), a star whose outlet takes 299
+    upstream reaches, a single reach; zero coefficients' segments (invalid
+    parameters) mixed in."""
+    rng = np.random.default_rng(R + 1)
+    if kind == "chain":
+        up_ptr, up_idx = [0] + list(range(R)), list(range(R - 1))
+    elif kind == "star":
+        up_ptr, up_idx = [0] * R + [R - 1], list(range(R - 1))
+    else:
+        up_ptr, up_idx = [0, 0], []
+    seg_len = rng.integers(1, 7, R).astype(np.int32)
+    topo = {"n_segments": int(seg_len.sum()), "reach_seg_start": np.concatenate([[0], np.cumsum(seg_len)[:-1]]).astype(np.int32),
+            "reach_seg_len": seg_len, "reach_up_ptr": np.array(up_ptr, np.int32), "reach_up_idx": np.array(up_idx, np.int32)}
+    S = topo["n_segments"]
+    _, p32, _, _ = synthetic(seed=17, segs=3000, n_ts=1)
+    p32 = np.ascontiguousarray(p32[rng.integers(0, len(p32), S)])
+    p32[rng.random(S) < 0.03, 4] = 0.0   # n_ch = 0
+    co = O.linear_coeffs(p32)
+    for a, b in zip(co, O.linear_coeffs(p32, use_ref=True)):
+        np.testing.assert_array_equal(a, b)
+    ql = rng.uniform(0.0, 2.0, (8, S)).astype(np.float32)
+    q0 = rng.uniform(0.0, 15.0, S).astype(np.float32)
+    np.testing.assert_array_equal(O.linear_route(co, topo, ql, q0), O.linear_route(co, topo, ql, q0, use_ref=True))
+
+
 @pytest.mark.gpu
 def test_gpu_matches_golden_and_oracle_bit_for_bit():
     n, topo = refnet()
