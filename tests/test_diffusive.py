@@ -36,6 +36,23 @@ def test_oracle_matches_compiled_reference_other_seed():
                                   O.diffusive_tridiag(rp, dx, diff, qp, use_ref=True, celerity=cel))
 
 
+@pytest.mark.skipif(not O.ref_available(), reason="needs the reference checkout (compiled reference)")
+def test_oracle_matches_compiled_reference_at_the_edges():
+    """Reaches of 1, 2 and 3 nodes and of the maximum 500, theta 0 and 1,
+    diffusivity and dx below the solver's floors, zero discharge: the oracle
+    against the reference's cpu_diffusive_tridiag, bit for bit."""
+    rp, dx, diff, cel, qp = MD.diffusive_inputs(n_reaches=64, seed=91)
+    rng = np.random.default_rng(92)
+    rp["ncomp"][:8] = [1, 2, 3, 500, 2, 500, 4, 1]
+    rp["theta"][8:16] = 0.0
+    rp["theta"][16:24] = 1.0
+    diff[24:32] = rng.uniform(0.0, 0.02, diff[24:32].shape)   # below the 0.01 floor for some nodes
+    dx[32:40] = rng.uniform(0.0, 2.0, dx[32:40].shape)        # below the 1 m floor for some nodes
+    qp[40:48] = 0.0
+    np.testing.assert_array_equal(O.diffusive_tridiag(rp, dx, diff, qp),
+                                  O.diffusive_tridiag(rp, dx, diff, qp, use_ref=True, celerity=cel))
+
+
 def test_bad_ncomp_rejected_by_the_library():
     rp, dx, diff, cel, qp = MD.diffusive_inputs(n_reaches=8)
     rp["ncomp"][1] = 0
