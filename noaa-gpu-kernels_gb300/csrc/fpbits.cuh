@@ -33,16 +33,11 @@ __device__ __forceinline__ bool fp_lt0(double x)
 // x == 0 (either sign)
 __device__ __forceinline__ bool fp_eq0(double x) { return ((unsigned long long)dbits(x) << 1) == 0; }
 
-// x > c and x >= c for a constant or value c > 0 that is not NaN
+// x > c for a constant or value c > 0 that is not NaN
 __device__ __forceinline__ bool fp_gt_pos(double x, double c)
 {
     const long long b = dbits(x);
     return b > dbits(c) && b <= kInfBits;
-}
-__device__ __forceinline__ bool fp_ge_pos(double x, double c)
-{
-    const long long b = dbits(x);
-    return b >= dbits(c) && b <= kInfBits;
 }
 
 // x >= c for c >= +0 (not NaN, not -0); x >= +0 is true for x = -0 as well

@@ -96,15 +96,6 @@ __device__ __forceinline__ void stage_seg_async(const NetDev& net, const RunDev&
     prefetch_l2(net.d + s);
 }
 
-// Lateral inflow of segment s in the step whose inflow row is qlat_row: the
-// record's column and scale, read as one 16-byte load {scale, column | pad}.
-__device__ __forceinline__ double seg_inflow(const NetDev& net, long long s, const double* qlat_row)
-{
-    const double2 qs = __ldg(reinterpret_cast<const double2*>(&net.seg[s].qscale));
-    const int col = (int)(unsigned)(__double_as_longlong(qs.y) & 0xffffffffll);   // qcol, the low word
-    return __ldg(qlat_row + col) * qs.x;
-}
-
 __device__ __forceinline__ SegP staged_seg(const double2* slot)
 {
     const double2 a = slot[0], b = slot[kSegSmemStride], c = slot[2 * kSegSmemStride];

@@ -53,13 +53,6 @@ __device__ __forceinline__ float pos_to_float(double v)
     return __int_as_float(((e - 896) << 23) | (int)((b >> 29) & 0x7fffff));
 }
 
-// A positive normal float as the equal double, on the integer pipe.
-__device__ __forceinline__ double widen_pos(float f)
-{
-    const unsigned fb = __float_as_uint(f);
-    return __longlong_as_double(((long long)((fb >> 23) + 896) << 52) | ((long long)(fb & 0x7fffff) << 29));
-}
-
 // Raw input -> feature: log of the value (flows offset by kFlowFloor m3/s, which
 // may be zero), standardised with the training set's mean / standard deviation.
 __device__ __forceinline__ float warm_feature(float x, bool flow, float mu, float inv_sd)
