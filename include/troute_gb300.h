@@ -185,6 +185,15 @@ int troute_route_tree(const troute_topo* topo, const troute_chparams* params,
                       const troute_cfg* cfg,
                       double* q_out, double* d_out, double* v_out,
                       double* reach_last_out, troute_stats* stats);
+/* The same call under the name the tree form's drop-in boundary was
+ * specified with (cpu_wavefront_fp64's semantics, WF/wavefront_mc.cu:495-507,
+ * in FP64 with a configuration and statistics). */
+int troute_mc_route_tree(const troute_topo* topo, const troute_chparams* params,
+                         const double* qlat_ts, const double* qdp0, const double* dp0,
+                         const double* reach_last0, int n_ts, double dt,
+                         const troute_cfg* cfg,
+                         double* q_out, double* d_out, double* v_out,
+                         double* reach_last_out, troute_stats* stats);
 
 /* ---- persistent network handle ---------------------------------------- */
 /* Builds the device schedule and uploads parameters (AoS, user order). */

@@ -468,6 +468,17 @@ extern "C" int troute_route_tree(const troute_topo* topo, const troute_chparams*
     return rc;
 }
 
+extern "C" int troute_mc_route_tree(const troute_topo* topo, const troute_chparams* params,
+                                    const double* qlat_ts, const double* qdp0, const double* dp0,
+                                    const double* reach_last0, int n_ts, double dt,
+                                    const troute_cfg* cfg,
+                                    double* q_out, double* d_out, double* v_out,
+                                    double* reach_last_out, troute_stats* stats)
+{
+    return troute_route_tree(topo, params, qlat_ts, qdp0, dp0, reach_last0, n_ts, dt, cfg, q_out, d_out, v_out,
+                             reach_last_out, stats);
+}
+
 extern "C" int troute_wavefront_fp64(const troute_chparams_f32* params,
                                      const int* reach_seg_start, const int* reach_seg_len,
                                      const int* reach_up_ptr, const int* reach_up_idx,

@@ -131,6 +131,7 @@ _SIGS = {
     "troute_mc_reach_parallel_device_noalloc": ([_P] * 10 + [_D, _D, _I, _I, _P, _P, _P], _I),
     "troute_wavefront_fp64": ([_P] * 7 + [_I, _I, _I] + [_P] * 6 + [_I, _D], _I),
     "troute_route_tree": ([_P] * 6 + [_I, _D, _P] + [_P] * 5, _I),
+    "troute_mc_route_tree": ([_P] * 6 + [_I, _D, _P] + [_P] * 5, _I),
     "troute_create": ([_P, _P, _P, _D, _P], _I),
     "troute_create_batch": ([_P, _I, _P, _P, _P, _P, _I, _D, _P], _I),
     "troute_create_ensemble": ([_P, _P, _P, _I, _P, _P, _D, _P], _I),

@@ -80,6 +80,22 @@ def test_no_device_is_reported_not_faked():
     with pytest.raises(T.TrouteError):
         T.mc_reach_parallel(c["params"], c["qlat"][0], t["reach_seg_start"], t["reach_seg_len"], c["q0"], c["q0"],
                             c["d0"])
+    # the tree form under both of its names, called through the C ABI directly
+    from troute_gb300 import api
+
+    arrs = [np.ascontiguousarray(t[k], np.int32) for k in ("reach_seg_start", "reach_seg_len", "reach_up_ptr",
+                                                             "reach_up_idx")]
+    topo, _keep = api._topo_struct(*arrs, t["n_segments"])
+    S = t["n_segments"]
+    p = np.ascontiguousarray(c["params"])   # structured ChParams records (64 B each)
+    ql = np.ascontiguousarray(c["qlat"], np.float64)
+    q0, d0 = np.ascontiguousarray(c["q0"], np.float64), np.ascontiguousarray(c["d0"], np.float64)
+    q = np.zeros(S)
+    for name in ("troute_route_tree", "troute_mc_route_tree"):
+        rc = getattr(T.lib(), name)(C.byref(topo), p.ctypes.data_as(C.c_void_p), ql.ctypes.data_as(C.c_void_p),
+                                    q0.ctypes.data_as(C.c_void_p), d0.ctypes.data_as(C.c_void_p), None, ql.shape[0],
+                                    300.0, None, q.ctypes.data_as(C.c_void_p), None, None, None, None)
+        assert rc in (6, 3), (name, rc)
 
 
 def test_bad_arguments_rejected_before_device():
