@@ -284,6 +284,21 @@ def workload(name: str, n_ts: int | None, members: tuple | None = None):
     return w
 
 
+def seeds_of(w: dict, model: bool = False) -> dict:
+    """The generator seeds of a workload, recorded in the JSON line's config:
+    the network's (or c2's basin set's), the ensemble members' perturbations,
+    and the warm-start model's initialisation and shuffling."""
+    if w.get("name") == "c2":
+        out = {"basins": 1002}
+    else:
+        out = {"network": w.get("seed")}
+    if "members" in w:
+        out["members"] = 1004
+    if model:
+        out["model"] = 1001
+    return out
+
+
 def shard(name: str, dist) -> tuple | None:
     """The rank's share of a batched workload (members or basins), or None
     (single networks run as replicas)."""
@@ -820,7 +835,7 @@ def run_ours(args, dist: Dist):
                        "first_timed_routed_step": args.warmup * n_ts,
                        "l2": f"inputs larger than L2 (129 MB): lateral inflow {w['qlat'].nbytes / 1e9:.2f} GB and "
                              f"segment parameters {S * 96 / 1e9:.2f} GB read per bench step",
-                       "parallelism": par},
+                       "parallelism": par, "seeds": seeds_of(w, bool(model))},
             "roofline": roofline, "critical_path": crit, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": (5 if model else 4) * args.steps, "parity": parity,
             "max_rel_err": None if parity is None else parity["max_rel_err"],

@@ -127,3 +127,18 @@ def test_profiles_carry_the_figures_the_bench_reads():
         assert sum(ln.strip().startswith(key + ":") for ln in text.splitlines()) == 1, (key, name)
         value, src = bench.profiled_file(key, name)
         assert src == name and value is not None and lo <= value <= hi, (key, name, value)
+
+
+def test_seeds_are_recorded_for_every_workload_form():
+    """The JSON line's config names the generator seeds: the network's (c1 is
+    seed 1010, 3,016 levels), the ensemble members' perturbations and the
+    warm-start model's."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.seeds_of(bench.workload("c0", 2)) == {"network": 1000}
+    assert bench.seeds_of(bench.workload("c1", 1)) == {"network": 1010}
+    assert bench.seeds_of(bench.workload("c3", 1), model=True) == {"network": 2006, "model": 1001}
+    assert bench.seeds_of(bench.workload("ens:2:2000:w", 2), model=True) == {"network": 7, "members": 1004,
+                                                                             "model": 1001}
+    assert bench.seeds_of({"name": "c2"}) == {"basins": 1002}
